@@ -1,0 +1,1 @@
+/* Empty stand-in: the emulated reference build uses no OpenGL. */
