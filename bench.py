@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""Benchmark of the SPH step: particle-steps/s on the 1,048,576-particle
+double dam break, with the HBM roofline of the dominant kernel.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step is one cSPH::Update (integrate, hash, sort, cell ranges, density,
+force) over all particles.  Inputs are synthetic and seeded
+(pibiti_gb300/configs.py).  Our arm times K steps with CUDA events on the
+handle's stream, each step started with a cold L2 (a 256 MiB buffer is
+written before each timed step, outside the events); `e2e` repeats the
+steps through the public API with positions and velocities uploaded from and
+read back to pinned host memory every step.  Under torchrun every rank runs
+an independent replica (the scene does not shard) and rank 0 prints one
+JSON line with the whole-job throughput.
+
+`--impl reference` times the CPU restatement of the reference's step (the
+oracle; the reference itself has no CPU path and its GPU code needs the
+reference tree) on all host cores, on a 131,072-particle sample of the same
+workload (two 64 x 16 x 64 columns, same spacing and constants).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s at 1M (plain vs learned, ≤1% density err); % HBM roofline"
+UNIT = "particle-steps/s"
+# Algorithmic bytes per particle (and per cell) each stage moves, every array
+# read or written once (the per-kernel model).
+STAGE_BYTES = {  # stage: (bytes per particle, bytes per cell)
+    "integrate_count": (40, 12),
+    "scan": (0, 8),
+    "scatter_ids": (20, 0),
+    "place": (88, 0),
+    "density": (24, 8),
+    "force": (56, 8),
+}
+KERNELS_PER_STEP = 7  # integrate_count, 2 scan kernels, scatter_ids, place, density, force
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
+    summary (profiles/), scaled to this workload there; None if absent."""
+    path = os.path.join(ROOT, "profiles", "force_double_dambreak_1M.md")
+    if not os.path.exists(path):
+        return None, None
+    kernel, val = None, None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            val = float(line.split(":")[1].split()[0])
+        if line.startswith("kernel:"):
+            kernel = line.split(":", 1)[1].strip()
+    return kernel, val
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.gpu = gpu_index
+        self.out = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_sample_workload():
+    from pibiti_gb300 import configs
+    return configs.dambreak_double(ny=16)
+
+
+def time_cpu_oracle(budget_s: float, min_steps: int = 3):
+    """Oracle (single-precision restatement) steps on the 131,072-particle
+    sample until `budget_s` of CPU work; returns (particle-steps/s, steps, threads)."""
+    import oracle
+    from pibiti_gb300.sph import Scene
+    w = cpu_sample_workload()
+    p = Scene.parse(w.xml).params
+    pos, vel = oracle.step(p, w.pos, w.vel, steps=1)  # warm-up (allocations, page-in)
+    steps, t = 0, 0.0
+    while steps < min_steps or t < budget_s:
+        t0 = time.perf_counter()
+        pos, vel = oracle.step(p, pos, vel, steps=1)
+        t += time.perf_counter() - t0
+        steps += 1
+    return w.n * steps / t, steps, oracle.threads(), w.n
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    from pibiti_gb300.sph import Scene
+    w = cpu_sample_workload()
+    p = Scene.parse(w.xml).params
+    pos, vel = w.pos, w.vel
+    for _ in range(args.warmup):
+        pos, vel = oracle.step(p, pos, vel, steps=1)
+    t0 = time.perf_counter()
+    pos, vel = oracle.step(p, pos, vel, steps=args.steps)
+    dt = time.perf_counter() - t0
+    value = w.n * args.steps / dt
+    threads = oracle.threads()
+    sample = (f"{w.n} particles (two 64x16x64 columns of the double dam break, same spacing, "
+              f"h and constants), {args.steps} full steps")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": workload_config(None),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "notes": "The reference has no CPU implementation of its step; this is the oracle's "
+                 "single-precision restatement of it (oracle/sph_oracle.c), OpenMP on all "
+                 "host threads.",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(p, n=None):
+    cfg = {"workload": "double dam break, 1,048,576 particles: two 64x128x64 lattices at "
+                       "spacing 0.5h (h=0.0457 m) in a 6.0x3.4x1.7 m box, +-1% jitter, "
+                       "rho0=1000, k=3, mu=3.5, g=-9.8, dt=1e-3, maxParInCell=16",
+           "particles": 1048576}
+    if p is not None:
+        cfg.update({"cells": int(p.numCells), "grid": [int(p.gridSize.x), int(p.gridSize.y),
+                                                         int(p.gridSize.z)],
+                    "l2": "flushed before every timed step (256 MiB write)"})
+    return cfg
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--warm-steps", type=int, default=200)
+    ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from pibiti_gb300 import configs
+    from pibiti_gb300.sph import ARRAY_POS, ARRAY_VEL, SPH, Scene
+
+    # CPU baseline first (no GPU work has started; rank 0 at N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_budget > 0:
+        v, steps, threads, n = time_cpu_oracle(args.cpu_budget)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{n} particles (two 64x16x64 columns of the same dam break), "
+                         f"{steps} full steps, oracle single-precision restatement"}
+
+    w = configs.dambreak_double(seed=42 + rank)
+    p = Scene.parse(w.xml).params
+    stream = torch.cuda.Stream()
+    sysm = SPH(p, stream=stream)
+    sysm.set_array(ARRAY_POS, w.pos)
+    sysm.set_array(ARRAY_VEL, w.vel)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    with torch.cuda.stream(stream):
+        sysm.update(args.warmup)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)
+            starts[k].record(stream)
+            sysm.update(1)
+            ends[k].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    total_ms = float(t.item())
+    n = sysm.n
+    value = world * n * args.steps / (total_ms / 1e3)
+
+    # warm multi-step throughput (graph replay, L2 not flushed): informative
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    warm_steps = max(args.warm_steps, 2)
+    e0.record(stream)
+    sysm.update(warm_steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    warm_ms = e0.elapsed_time(e1) / warm_steps
+
+    # per-stage times (CUDA events on the handle's stream), cold L2
+    stages = {k: [] for k in SPH.STAGES}
+    for _ in range(20):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        for k, v in sysm.step_timed().items():
+            stages[k].append(v)
+    stage_ms = {k: statistics.median(v) for k, v in stages.items()}
+    dom = max(stage_ms, key=stage_ms.get)
+    bp, bc = STAGE_BYTES[dom]
+    alg = bp * n + bc * p.numCells
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (stage_ms[dom] / 1e3) / 1e9
+    kname, traffic = ncu_traffic()
+    roofline = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "algorithmic_bytes": alg, "peak_source": peak_kind,
+                "stage_ms": stage_ms}
+    P = 4 if p.numCells >= 65536 else 2
+    model_b = 256 + 24 * P + 12 * p.numCells / n
+    step_gbs = model_b * n / (total_ms / args.steps / 1e3) / 1e9
+    roofline_step = {"bytes_per_particle_step": model_b, "achieved": step_gbs, "peak": peak,
+                     "unit": "GB/s", "frac": step_gbs / peak,
+                     "note": "reference dataflow byte model B = 256 + 24P + 12C/N"}
+
+    # end to end through the public API with pinned host buffers
+    hpos = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    hvel = torch.empty((n, 4), dtype=torch.float32).pin_memory()
+    sysm.get_array(ARRAY_POS, hpos.numpy())
+    sysm.get_array(ARRAY_VEL, hvel.numpy())
+    es, ee = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    es.record(stream)
+    for _ in range(args.e2e_steps):
+        sysm.set_array(ARRAY_POS, hpos.numpy())
+        sysm.set_array(ARRAY_VEL, hvel.numpy())
+        sysm.update(1)
+        sysm.get_array(ARRAY_POS, hpos.numpy())
+        sysm.get_array(ARRAY_VEL, hvel.numpy())
+    ee.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = es.elapsed_time(ee)
+    t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = world * n * args.e2e_steps / (float(t.item()) / 1e3)
+
+    st = sysm.stats()[0]
+    flags = sysm.flags()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(p),
+            "parallelism": f"replicas x{world}" if world > 1 else "single",
+            "e2e": {"value": e2e_value, "unit": UNIT, "steps": args.e2e_steps,
+                    "h2d_bytes_per_step": 2 * n * 16, "d2h_bytes_per_step": 2 * n * 16},
+            "roofline": roofline, "roofline_step": roofline_step,
+            "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": KERNELS_PER_STEP * args.steps,
+            "warm_ms_per_step": warm_ms,
+            "wall_s_timed_loop": wall,
+            "state_check": {"kinetic_energy": st[0], "mean_density": st[1],
+                            "max_density_dev": st[2], "nonfinite": st[3], "flags": flags},
+        }
+        print(json.dumps(line), flush=True)
+    sysm.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

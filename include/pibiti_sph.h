@@ -1,0 +1,220 @@
+/*
+ * pibiti_sph.h -- C ABI of the GB300 SPH step (libpibiti_sph.so).
+ *
+ * Two layers, both plain C with no CUDA or torch types in the signatures
+ * (streams are passed as `void*` holding a cudaStream_t; NULL means the
+ * legacy default stream):
+ *
+ *  1. Stage entry points with the argument lists of the reference's own
+ *     extern "C" wrappers (source/CUDA/System.cuh:1-38,
+ *     source/CUDA/radixsort.cuh:67-69), with OpenGL buffer ids replaced by
+ *     device pointers.  A program that called the reference's wrappers calls
+ *     these in the same order (cSPH::Update, source/SPH/SPH_Update.cpp:12-81)
+ *     and gets the same buffers back.  Device buffers belong to the caller.
+ *
+ *  2. A system handle (the replacement for cSPH, source/SPH/SPH.h:9-50)
+ *     that owns its device buffers and runs whole steps with fused kernels:
+ *     sph_create / sph_set_array / sph_get_array / sph_step / sph_destroy.
+ *     One handle can hold many independent scenes (an ensemble) stepped
+ *     together.
+ *
+ * Every function returns an int status (SPH_OK = 0).  The reference exits
+ * the process on any CUDA error (cutil.h CUDA_SAFE_CALL); this library
+ * returns SPH_ERR_CUDA instead and sph_last_error() describes it.
+ * Calls are asynchronous on their stream unless stated otherwise.
+ */
+#ifndef PIBITI_SPH_H
+#define PIBITI_SPH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "sph_params.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SPH_OK 0
+#define SPH_ERR_CUDA 1        /* a CUDA call failed (context may be unusable) */
+#define SPH_ERR_ARG 2         /* bad pointer, size or index */
+#define SPH_ERR_PARAMS 3      /* SimParams inconsistent or outside what the kernels cover */
+#define SPH_ERR_UNSUPPORTED 4 /* a reference feature this library does not implement */
+#define SPH_ERR_TIMEOUT 5     /* a bounded device wait gave up */
+#define SPH_ERR_NOMEM 6       /* device or host allocation failed */
+#define SPH_ERR_STATE 7       /* call not valid in the current state */
+#define SPH_ERR_XML 8         /* scene file missing or malformed */
+
+/* Text of the last error raised on the calling host thread. */
+const char* sph_last_error(void);
+/* Library version string. */
+const char* sph_version(void);
+
+/* ======================================================================
+ * 1. Stage entry points (reference wrappers)
+ * ==================================================================== */
+
+/* threadSync (System.cu:613): wait for all device work. */
+int sph_threadSync(void);
+/* allocateArray / freeArray (System.cu:616-617). */
+int sph_allocateArray(void** devPtr, size_t size);
+int sph_freeArray(void* devPtr);
+/* copyFromDevice (System.cu:623-628) without the VBO id; copyToDevice
+   (System.cu:629-632).  Synchronous, like the reference. */
+int sph_copyFromDevice(void* host, const void* device, int size);
+int sph_copyToDevice(void* device, const void* host, int offset, int size);
+
+/* setParameters (System.cu:634-637): the parameters every following stage
+   call uses (one set per process, like the reference's __constant__ par).
+   Rejects parameter sets the kernels do not cover (SPH_ERR_PARAMS /
+   SPH_ERR_UNSUPPORTED). */
+int sph_setParameters(const SimParams* hostParams);
+/* Stream for the stage calls (NULL: legacy default stream). */
+int sph_setStageStream(void* stream);
+
+/* integrate (System.cuh:24-25): integrateD + boundary() over all particles,
+   old -> new position and velocity (float4, original order). */
+int sph_integrate(const sph_float4* oldPos, sph_float4* newPos, const sph_float4* oldVel,
+                  sph_float4* newVel, int numParticles);
+
+/* calcHash (System.cuh:27): particleHash[i] = {cell hash of pos[i], i}. */
+int sph_calcHash(const sph_float4* pos, sph_uint2* particleHash, int numParticles);
+
+/* RadixSort (radixsort.cuh:67-69, radixsort_kernel.cu:445-472): stable sort
+   of (key, value) pairs by the low `bits` bits of the key, 8 bits per pass,
+   ping-ponging between pData0 and pData1.  After an even number of passes
+   (bits = 16 or 32, the values cSPH::Update uses) the result is in pData0;
+   after an odd number it is in pData1, exactly as with the reference. */
+int sph_RadixSort(sph_uint2* pData0, sph_uint2* pData1, uint32_t elements, uint32_t bits);
+
+/* reorder (System.cuh:29-30): cellStart[c] = first sorted index of cell c
+   (0xFFFFFFFF when empty), pos/vel gathered into sorted order. */
+int sph_reorder(const sph_float4* oldPos, const sph_float4* oldVel, sph_float4* sortedPos,
+                sph_float4* sortedVel, const sph_uint2* particleHash, uint32_t* cellStart,
+                uint32_t numParticles, uint32_t numCells);
+
+/* collide (System.cuh:32-35) without the timer and GL ids: density pass
+   (pressure, density in sorted order), then force pass writing
+   newVel[particleHash[i].y].  clr (may be NULL) and dyeColor (may be NULL)
+   receive the colour and dye outputs in original order; oldPos/newPos/
+   oldVel are accepted for signature parity and not read, as in the
+   reference's kernels. */
+int sph_collide(const sph_float4* oldPos, sph_float4* newPos, sph_float4* clr,
+                const sph_float4* sortedPos, const sph_float4* sortedVel, const sph_float4* oldVel,
+                sph_float4* newVel, float* pressure, float* density, float* dyeColor,
+                const sph_uint2* particleHash, const uint32_t* cellStart, uint32_t numParticles,
+                uint32_t numCells);
+
+/* ======================================================================
+ * 2. System handle (cSPH replacement)
+ * ==================================================================== */
+typedef struct SphSystem SphSystem;
+
+#define SPH_ARRAY_POS 0
+#define SPH_ARRAY_VEL 1
+
+/* Create a system for one scene of params->numParticles particles
+   (cSPH::_InitMem, SPH_Mem.cpp:11-54).  Particles start at the origin with
+   zero velocity until sph_set_array fills them. */
+int sph_create(const SimParams* params, SphSystem** out);
+/* Create one system holding `count` independent scenes, stepped together. */
+int sph_create_ensemble(const SimParams* scenes, uint32_t count, SphSystem** out);
+int sph_destroy(SphSystem* sys);
+/* Stream used by every following call on this handle. */
+int sph_set_stream(SphSystem* sys, void* stream);
+/* Replace a scene's parameters between steps (the slider path of
+   SPH_Update.cpp:19-26).  numParticles and the grid must not change. */
+int sph_set_params(SphSystem* sys, uint32_t scene, const SimParams* params);
+int sph_get_params(SphSystem* sys, uint32_t scene, SimParams* out);
+uint32_t sph_num_scenes(const SphSystem* sys);
+/* Total particles (all scenes) and the first particle index of a scene. */
+uint32_t sph_num_particles(const SphSystem* sys);
+uint32_t sph_scene_offset(const SphSystem* sys, uint32_t scene);
+
+/* setArray (SPH_Util.cpp:59-71): write `count` float4 records, starting at
+   original particle index `start` (indices run over all scenes), from host
+   memory (src_on_device = 0) or device memory (1).  Synchronous for host
+   sources. */
+int sph_set_array(SphSystem* sys, uint32_t which, const sph_float4* data, uint32_t start,
+                  uint32_t count, int src_on_device);
+/* getArray (SPH_Util.cpp:44-56): all particles in original order, to host
+   (dst_on_device = 0, synchronous) or device memory.  `which` is an enum;
+   the reference's inverted bool is not reproduced. */
+int sph_get_array(SphSystem* sys, uint32_t which, sph_float4* out, int dst_on_device);
+
+/* Update (SPH_Update.cpp:12-81) `steps` times: integrate, hash, sort,
+   cell ranges, density, force.  Steps after the first replay a captured
+   CUDA graph. */
+int sph_step(SphSystem* sys, uint32_t steps);
+
+/* One step with a CUDA event recorded on the handle's stream before the
+   first stage and after each of the six stages (1: integrate + cell count,
+   2: scan, 3: id scatter, 4: stable placement, 5: density, 6: force);
+   stage_ms[k] receives stage k+1's time in ms.  Synchronous. */
+int sph_step_timed(SphSystem* sys, float* stage_ms, uint32_t nstages);
+
+/* The neighbour structures of the last step, in the reference's formats:
+   sortedHash[i] = {cell hash, original index} (local to each scene),
+   cellStart[c] (0xFFFFFFFF when empty) and cellEnd[c] (one past the last
+   sorted index; 0xFFFFFFFF when empty), cells of all scenes concatenated.
+   Any pointer may be NULL.  To host (synchronous) or device memory. */
+int sph_get_cells(SphSystem* sys, sph_uint2* sortedHash, uint32_t* cellStart, uint32_t* cellEnd,
+                  int dst_on_device);
+/* Density and pressure of the last step, in sorted order (as the reference
+   keeps dDensity/dPressure), to host or device memory. */
+int sph_get_fields(SphSystem* sys, float* density, float* pressure, int dst_on_device);
+uint32_t sph_num_cells(const SphSystem* sys);
+
+/* Double-precision reductions of the current state, per scene:
+   out[4*s + 0] kinetic energy, [1] mean density of the last step,
+   [2] max |rho/rho0 - 1|, [3] number of non-finite position/velocity
+   components.  Synchronous. */
+int sph_stats(SphSystem* sys, double* out);
+
+/* Error and counter flags raised on the device since the last call (and
+   cleared by it): bit 0 a cell held more than maxParInCell particles (the
+   walk truncated it, as the reference does), bit 1 a non-finite position. */
+int sph_flags(SphSystem* sys, uint32_t* flags);
+
+/* ======================================================================
+ * 3. Scenes (Scene / cSPH::LoadScenes replacement, host only)
+ * ==================================================================== */
+
+/* Init data of a scene that is not part of SimParams (Scene.h:22-62). */
+typedef struct {
+  char title[64];
+  int32_t chapter, is_default;
+  float cellSize;
+  sph_float3 initMin, initMax;
+  int32_t initType, initLast;
+  float spacing, dropR;
+  int32_t rain;
+} SphSceneInfo;
+
+/* Number of <Scene> elements under the root of a Scenes.xml file. */
+int sph_scene_count(const char* path, int* count);
+/* Scene `index` of the file: the reference's defaults (Scene.cpp:7-66),
+   the XML attributes (Scene_Load.cpp:11-111) and the derived constants
+   (Scene.cpp:69-113).  info may be NULL. */
+int sph_scene_load(const char* path, int index, SimParams* out, SphSceneInfo* info);
+/* The same for one <Scene .../> element given as text. */
+int sph_scene_parse(const char* xml, SimParams* out, SphSceneInfo* info);
+/* Scene() with no XML: defaults plus derivations. */
+int sph_scene_default(SimParams* out, SphSceneInfo* info);
+/* Index of the scene marked default="" (or def=""), else 0
+   (SPH_Scenes.cpp:186). */
+int sph_scene_default_index(const char* path, int* index);
+
+/* cSPH::Reset (SPH_Init.cpp:23-79): the initial volume of a scene, written
+   to host arrays of numParticles float4 each.  type 0 fills the init volume
+   as a lattice (the reference's loop order); type 1 places particles
+   uniformly at random from a seeded generator (the reference calls
+   rand()).  Returns the number of particles placed in *placed. */
+int sph_scene_reset(const SimParams* params, const SphSceneInfo* info, int type, uint64_t seed,
+                    sph_float4* pos, sph_float4* vel, uint32_t* placed);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PIBITI_SPH_H */

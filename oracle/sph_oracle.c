@@ -58,7 +58,11 @@ static inline uint32_t fetch_cell_start(const uint32_t* cs, uint32_t num_cells, 
   return (x >= 0 && (uint32_t)x < num_cells) ? cs[x] : 0u;
 }
 
-/* FETCH(particleHash, j).x through a texture bound to n entries. */
+/* FETCH(particleHash, j).x through a texture bound to n entries.  The
+   walks stop at j >= n: there the reference's texture returns a zero key and
+   zero particle, which a walk of cell 0 would take for a particle at the
+   origin (only when every particle sits in cell 0); the oracle and the
+   product stop instead. */
 static inline uint32_t fetch_key(const uint32_t* kv, uint32_t n, uint32_t j) {
   const int32_t x = (int32_t)j;
   return (x >= 0 && (uint32_t)x < n) ? kv[2 * (size_t)x] : 0u;

@@ -1,0 +1,419 @@
+// sph_device.cuh -- per-particle device math shared by every SPH kernel.
+//
+// Each function restates one piece of the reference's device code (cited on
+// the function).  The translation units that include this header are built
+// with --fmad=false, so every multiply and add rounds separately exactly as
+// written; the few fused multiply-adds are explicit __fmaf_rn calls, and
+// divisions and square roots are the IEEE round-to-nearest intrinsics.  The
+// arithmetic is therefore a fixed sequence of IEEE operations.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "sph_params.h"
+
+namespace sph {
+
+constexpr uint32_t kEmpty = 0xffffffffu;
+
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ float len3(float3 a) { return __fsqrt_rn(dot3(a, a)); }
+__device__ __forceinline__ float len2(float x, float y) {
+  return __fsqrt_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)));
+}
+
+// __mul24 semantics: product of the low 24 bits of each operand, signed.
+__device__ __forceinline__ int mul24(int a, int b) { return __mul24(a, b); }
+
+// calcGridPos (Kernel_Cell.cui:5-13): floor((p - worldMin) / cellSize).
+// float->int conversion saturates and maps NaN to 0, as cvt.rmi does.
+__device__ __forceinline__ int3 grid_pos(const SimParams& p, float4 x) {
+  const float gx = __fdiv_rn(__fsub_rn(x.x, p.worldMin.x), p.cellSize.x);
+  const float gy = __fdiv_rn(__fsub_rn(x.y, p.worldMin.y), p.cellSize.y);
+  const float gz = __fdiv_rn(__fsub_rn(x.z, p.worldMin.z), p.cellSize.z);
+  return make_int3(__float2int_rd(gx), __float2int_rd(gy), __float2int_rd(gz));
+}
+
+// calcGridHash (Kernel_Cell.cui:15-19), including its wrap-around for
+// coordinates outside the grid.
+__device__ __forceinline__ uint32_t grid_hash_raw(const SimParams& p, int x, int y, int z) {
+  return (uint32_t)(mul24(z, (int)p.gridSize_yx) + mul24(y, (int)p.gridSize.x) + x);
+}
+
+// Cell index of a position, clamped into the grid.  Identical to the raw hash
+// for every position inside the world box; a position outside it (only
+// possible for NaN or for data placed outside the box by the caller) lands in
+// the nearest cell instead of an aliased or out-of-range one.
+__device__ __forceinline__ uint32_t cell_of(const SimParams& p, int3 g) {
+  const int x = min(max(g.x, 0), (int)p.gridSize.x - 1);
+  const int y = min(max(g.y, 0), (int)p.gridSize.y - 1);
+  const int z = min(max(g.z, 0), (int)p.gridSize.z - 1);
+  return (uint32_t)(z * (int)p.gridSize_yx + y * (int)p.gridSize.x + x);
+}
+
+// One soft wall of boundary() (System.cu:52-53, addB/addC):
+// acc = stiff*diff - damp*dot(n, v); v += acc * n * dt.
+__device__ __forceinline__ void add_wall(float3& v, float3 n, float diff, float stiff, float damp,
+                                         float dt) {
+  const float acc = __fsub_rn(__fmul_rn(stiff, diff), __fmul_rn(damp, dot3(n, v)));
+  v.x = __fadd_rn(v.x, __fmul_rn(__fmul_rn(acc, n.x), dt));
+  v.y = __fadd_rn(v.y, __fmul_rn(__fmul_rn(acc, n.y), dt));
+  v.z = __fadd_rn(v.z, __fmul_rn(__fmul_rn(acc, n.z), dt));
+}
+
+// boundary() (System.cu:41-159): every boundary type and z effect.
+__device__ inline void boundary(const SimParams& p, float3& pos, float3& vel) {
+  float3 wmin = p.worldMin, wmax = p.worldMax;
+  const float b = p.distBndSoft, stiff = p.bndStiff, damp = p.bndDamp, damp2 = p.bndDampC;
+  const float dt = p.timeStep;
+  const float EPS = 0.00001f;
+  const uint32_t t = p.bndType;
+  const bool bCylY = t == SPH_BND_CYL_Y, bCylZ = t == SPH_BND_CYL_Z;
+  const bool bWave = p.bndEffZ == SPH_BND_EFF_WAVE, bNoEff = p.bndEffZ == SPH_BND_EFF_NONE,
+             bCycle = p.bndEffZ == SPH_BND_EFF_CYCLE;
+  float diff;
+  if (bWave) {
+    const float sl = -p.r2Angle;
+    diff = __fsub_rn(__fsub_rn(b, __fsub_rn(pos.y, wmin.y)), __fmul_rn(__fsub_rn(pos.z, wmin.z), sl));
+    if (diff > EPS) add_wall(vel, f3(0.f, __fsub_rn(1.f, sl), sl), diff, stiff, damp, dt);
+    wmin.z = __fadd_rn(wmin.z, __fmul_rn(p.rTwist, __fadd_rn(1.f, sinf(p.rAngle))));
+  }
+  if (t != SPH_BND_SPHERE) {
+    if (!bCylY) {
+      if (bNoEff || bWave) {
+        diff = __fadd_rn(__fsub_rn(b, pos.z), wmin.z);
+        if (diff > EPS) add_wall(vel, f3(0.f, 0.f, 1.f), diff, stiff, damp2, dt);
+      }
+      if (!bCycle) {
+        diff = __fsub_rn(__fadd_rn(b, pos.z), wmax.z);
+        if (diff > EPS) add_wall(vel, f3(0.f, 0.f, -1.f), diff, stiff, damp2, dt);
+      }
+    }
+    if (!bCylY && !bCylZ) {
+      diff = __fadd_rn(__fsub_rn(b, pos.x), wmin.x);
+      if (diff > EPS) add_wall(vel, f3(1.f, 0.f, 0.f), diff, stiff, damp, dt);
+      diff = __fsub_rn(__fadd_rn(b, pos.x), wmax.x);
+      if (diff > EPS) add_wall(vel, f3(-1.f, 0.f, 0.f), diff, stiff, damp, dt);
+    }
+    if (!bCylZ) {
+      diff = __fadd_rn(__fsub_rn(b, pos.y), wmin.y);
+      if (diff > EPS) add_wall(vel, f3(0.f, 1.f, 0.f), diff, stiff, damp, dt);
+      diff = __fsub_rn(__fadd_rn(b, pos.y), wmax.y);
+      if (diff > EPS) add_wall(vel, f3(0.f, -1.f, 0.f), diff, stiff, damp, dt);
+    }
+  } else {
+    const float len = len3(pos);
+    diff = __fadd_rn(__fadd_rn(b, len), wmin.y);
+    if (diff > EPS)
+      add_wall(vel, f3(__fdiv_rn(-pos.x, len), __fdiv_rn(-pos.y, len), __fdiv_rn(-pos.z, len)),
+               diff, stiff, damp2, dt);
+  }
+  if (bCylY || t == SPH_BND_CYL_YZ) {
+    const float len = len2(pos.x, pos.z);
+    diff = __fsub_rn(__fadd_rn(b, len), wmax.x);
+    if (diff > EPS)
+      add_wall(vel, f3(__fdiv_rn(-pos.x, len), 0.f, __fdiv_rn(-pos.z, len)), diff, stiff, damp2, dt);
+  }
+  if (bCylZ || t == SPH_BND_CYL_YZ) {
+    const float len = len2(pos.x, pos.y);
+    diff = __fadd_rn(__fadd_rn(b, len), wmin.y);
+    if (diff > EPS)
+      add_wall(vel, f3(__fdiv_rn(-pos.x, len), __fdiv_rn(-pos.y, len), 0.f), diff, stiff, damp2, dt);
+  }
+  if (!bWave && !bNoEff) {
+    const float dr = __fmul_rn(1.f, p.particleR);
+    const float span = __fsub_rn(__fsub_rn(__fsub_rn(wmax.z, wmin.z), __fmul_rn(2.f, b)), dr);
+    if (bCycle && vel.z > p.rVexit && pos.z > __fsub_rn(__fsub_rn(wmax.z, b), dr))
+      pos.z = __fsub_rn(pos.z, span);
+    else if (vel.z < -p.rVexit && pos.z < __fadd_rn(__fadd_rn(wmin.z, b), dr))
+      pos.z = __fadd_rn(pos.z, span);
+  }
+  if (t == SPH_BND_PUMP_Y) {
+    const float PI2_ = 2.f * 3.141592654f;
+    const float rad = wmax.x, ang = p.angOut, hc = p.hClose, rin = __fmul_rn(rad, p.radIn);
+    const float len = len2(pos.x, pos.y);
+    const float3 nrad = f3(__fdiv_rn(-pos.x, len), __fdiv_rn(-pos.y, len), 0.f);
+    diff = __fsub_rn(__fadd_rn(b, len), rad);
+    if (diff > EPS) {
+      const float a = atanf(__fdiv_rn(pos.x, pos.y));
+      if (ang < 0.5f) {
+        if (a < -ang || a > ang || pos.y < 0) add_wall(vel, nrad, diff, stiff, damp, dt);
+      } else {
+        if (pos.y < 0 || (len < __fmul_rn(rad, p.s5) && a < ang)) add_wall(vel, nrad, diff, stiff, damp, dt);
+      }
+    }
+    float xs;
+    if (ang < 0.5f) {
+      xs = __fmul_rn(sinf(__fmul_rn(ang, p.s3)), rad);
+      const float zs = __fmul_rn(__fmul_rn(cosf(__fmul_rn(ang, p.s3)), rad), p.s4);
+      if (pos.y > zs) {
+        diff = __fsub_rn(__fsub_rn(b, pos.x), xs);
+        if (diff > EPS) add_wall(vel, f3(1.f, 0.f, 0.f), diff, stiff, damp, dt);
+        diff = __fsub_rn(__fadd_rn(b, pos.x), xs);
+        if (diff > EPS) add_wall(vel, f3(-1.f, 0.f, 0.f), diff, stiff, damp, dt);
+      }
+    } else {
+      xs = __fmul_rn(0.09f, p.s4);
+      if (len >= __fmul_rn(rad, p.s6)) {
+        diff = __fadd_rn(__fsub_rn(b, pos.x), xs);
+        if (diff > EPS) add_wall(vel, f3(1.f, 0.f, 0.f), diff, stiff, damp, dt);
+      }
+    }
+    if (pos.z > __fsub_rn(hc, __fmul_rn(b, p.s1))) {
+      diff = __fsub_rn(__fadd_rn(b, len), rin);
+      if (diff > EPS) add_wall(vel, nrad, diff, stiff, damp, dt);
+    }
+    if (pos.z < __fsub_rn(hc, __fmul_rn(b, p.s2))) {
+      diff = __fsub_rn(__fadd_rn(b, pos.z), hc);
+      if (diff > EPS) add_wall(vel, f3(0.f, 0.f, -1.f), diff, stiff, damp, dt);
+    }
+    diff = __fadd_rn(__fsub_rn(pos.y, wmax.y), p.rDexit);
+    if (diff > EPS && vel.y > p.rVexit) {
+      float aa, rr;
+      const float zz = fabsf(__fsub_rn(hc, wmin.z));
+      if (ang < 0.5f) {
+        const float xx = __fmul_rn(xs, 2.f);
+        rr = __fmul_rn(__fdiv_rn(__fadd_rn(pos.x, __fdiv_rn(xx, 2.f)), xx), 0.7f);
+        aa = __fmul_rn(__fdiv_rn(__fsub_rn(pos.z, __fdiv_rn(zz, 2.f)), zz), 1.6f);
+      } else {
+        rr = __fmul_rn(__fdiv_rn(__fsub_rn(wmax.x, pos.x), xs), 0.45f);
+        aa = __fmul_rn(__fdiv_rn(__fsub_rn(pos.z, __fdiv_rn(zz, 2.f)), zz), 1.8f);
+      }
+      rr = __fmul_rn(rr, rin);
+      aa = __fmul_rn(aa, PI2_);
+      const float x = __fmul_rn(cosf(aa), rr), y = __fmul_rn(sinf(aa), rr);
+      const float z = (float)__dsub_rn((double)__fsub_rn(wmax.z, b),
+                                       __dmul_rn((double)fabsf(__fsub_rn(vel.y, p.rVexit)), 0.01));
+      pos = f3(x, y, z);
+      vel = f3(vel.x, vel.z, -vel.y);
+    }
+  }
+}
+
+// integrateD (System.cu:165-205): boundary, v += g dt, v *= damping,
+// x += v dt, hard clamp.  w components are carried by the caller.
+__device__ __forceinline__ void integrate(const SimParams& p, float3& x, float3& v) {
+  boundary(p, x, v);
+  const float dt = p.timeStep, damp = p.globalDamping;
+  v.x = __fadd_rn(v.x, __fmul_rn(p.gravity.x, dt));
+  v.y = __fadd_rn(v.y, __fmul_rn(p.gravity.y, dt));
+  v.z = __fadd_rn(v.z, __fmul_rn(p.gravity.z, dt));
+  v.x = __fmul_rn(v.x, damp);
+  v.y = __fmul_rn(v.y, damp);
+  v.z = __fmul_rn(v.z, damp);
+  x.x = __fadd_rn(x.x, __fmul_rn(v.x, dt));
+  x.y = __fadd_rn(x.y, __fmul_rn(v.y, dt));
+  x.z = __fadd_rn(x.z, __fmul_rn(v.z, dt));
+  const float b = p.distBndHard;
+  const float hix = __fsub_rn(p.worldMax.x, b), lox = __fadd_rn(p.worldMin.x, b);
+  const float hiy = __fsub_rn(p.worldMax.y, b), loy = __fadd_rn(p.worldMin.y, b);
+  const float hiz = __fsub_rn(p.worldMax.z, b), loz = __fadd_rn(p.worldMin.z, b);
+  if (x.x > hix) x.x = hix;
+  if (x.x < lox) x.x = lox;
+  if (x.y > hiy) x.y = hiy;
+  if (x.y < loy) x.y = loy;
+  if (x.z > hiz) x.z = hiz;
+  if (x.z < loz) x.z = loz;
+}
+
+// Pair term of compDensCell (Kernel_Cell.cui:157-169): (h^2 - r^2)^3 when
+// r^2 < h^2, accumulated as acc + (c*c)*c with one fused step.
+__device__ __forceinline__ float density_pair(float4 a, float4 b, float h2, float acc, int& nbr) {
+  const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
+  const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+  if (r2 < h2) {
+    const float c = __fsub_rn(h2, r2);
+    acc = __fmaf_rn(__fmul_rn(c, c), c, acc);
+    ++nbr;
+  }
+  return acc;
+}
+
+// Constants of compForcePair hoisted out of the neighbour loop.
+struct ForceConsts {
+  float h, minDist, spiky, vterm, minDens;
+};
+__device__ __forceinline__ ForceConsts force_consts(const SimParams& p) {
+  ForceConsts k;
+  k.h = p.h;
+  k.minDist = p.minDist;
+  k.spiky = p.SpikyKern;
+  k.vterm = __fmul_rn(p.LapKern, p.viscosity);
+  k.minDens = p.minDens;
+  return k;
+}
+
+// compForceCell inner step + compForcePair (Kernel_Cell.cui:210-228,
+// 251-258): d12 = min(minDens, 1/(rho_i rho_j)); r = max(minDist, |x_i-x_j|);
+// if r < h: F += (c Spiky (p_i+p_j)/r (x_i-x_j) + Lap mu (v_j-v_i)) c d12.
+__device__ __forceinline__ void force_pair(const ForceConsts& k, float4 xi, float4 vi, float di,
+                                           float pi, float4 xj, float4 vj, float dj, float pj,
+                                           float3& acc) {
+  const float dd = __fdiv_rn(1.0f, __fmul_rn(di, dj));
+  const float d12 = fminf(k.minDens, dd);
+  const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
+  const float vx = __fsub_rn(vj.x, vi.x), vy = __fsub_rn(vj.y, vi.y), vz = __fsub_rn(vj.z, vi.z);
+  const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
+  const float r = fmaxf(k.minDist, __fsqrt_rn(dist2));
+  if (r < k.h) {
+    const float c = __fsub_rn(k.h, r);
+    const float pterm = __fdiv_rn(__fmul_rn(__fmul_rn(c, k.spiky), __fadd_rn(pi, pj)), r);
+    const float s = __fmul_rn(c, d12);
+    acc.x = __fadd_rn(acc.x, __fmul_rn(__fmaf_rn(pterm, rx, __fmul_rn(k.vterm, vx)), s));
+    acc.y = __fadd_rn(acc.y, __fmul_rn(__fmaf_rn(pterm, ry, __fmul_rn(k.vterm, vy)), s));
+    acc.z = __fadd_rn(acc.z, __fmul_rn(__fmaf_rn(pterm, rz, __fmul_rn(k.vterm, vz)), s));
+  }
+}
+
+// collideSpheres (Kernel_Cell.cui:78-96); float3/float is a multiply by the
+// reciprocal (cutil_math.h:358-362).
+__device__ __forceinline__ float3 collide_sphere(const SimParams& p, float3 rel, float3 rv,
+                                                 float radius) {
+  const float dist = len3(rel);
+  float3 f = f3(0.f, 0.f, 0.f);
+  if (dist < radius) {
+    const float inv = __fdiv_rn(1.0f, dist);
+    const float3 n = f3(__fmul_rn(rel.x, inv), __fmul_rn(rel.y, inv), __fmul_rn(rel.z, inv));
+    const float vn = dot3(rv, n);
+    const float3 tv = f3(__fsub_rn(rv.x, __fmul_rn(vn, n.x)), __fsub_rn(rv.y, __fmul_rn(vn, n.y)),
+                         __fsub_rn(rv.z, __fmul_rn(vn, n.z)));
+    const float sp = __fmul_rn(p.spring, __fsub_rn(dist, radius));
+    f.x = __fadd_rn(__fadd_rn(__fmul_rn(sp, n.x), __fmul_rn(p.damping, rv.x)), __fmul_rn(p.shear, tv.x));
+    f.y = __fadd_rn(__fadd_rn(__fmul_rn(sp, n.y), __fmul_rn(p.damping, rv.y)), __fmul_rn(p.shear, tv.y));
+    f.z = __fadd_rn(__fadd_rn(__fmul_rn(sp, n.z), __fmul_rn(p.damping, rv.z)), __fmul_rn(p.shear, tv.z));
+  }
+  return f;
+}
+
+// The part of computeForceD after the neighbour sums (System.cu:249-250,
+// 373-402): dv = F m dt, plus the sphere collider and the accelerators.
+__device__ inline float3 velocity_increment(const SimParams& p, float3 F, float4 xi, float4 vi) {
+  const float s = __fmul_rn(p.particleMass, p.timeStep);
+  float3 add = f3(__fmul_rn(F.x, s), __fmul_rn(F.y, s), __fmul_rn(F.z, s));
+  if (p.rotType <= 0) {
+    const float3 rel = f3(__fsub_rn(p.collPos.x, xi.x), __fsub_rn(p.collPos.y, xi.y),
+                          __fsub_rn(p.collPos.z, xi.z));
+    const float3 c = collide_sphere(p, rel, f3(-vi.x, -vi.y, -vi.z), __fadd_rn(p.particleR, p.collR));
+    add.x = __fadd_rn(add.x, c.x);
+    add.y = __fadd_rn(add.y, c.y);
+    add.z = __fadd_rn(add.z, c.z);
+  }
+#pragma unroll 1
+  for (int a = 0; a < SPH_NUM_ACC; ++a) {
+    const SphAccel& ac = p.acc[a];
+    if (ac.type == SPH_ACC_OFF) continue;
+    const float3 rel = f3(__fsub_rn(xi.x, ac.pos.x), __fsub_rn(xi.y, ac.pos.y), __fsub_rn(xi.z, ac.pos.z));
+    const float dt = p.timeStep;
+    if (ac.type == SPH_ACC_BOX) {
+      if (fabsf(rel.x) < ac.size.x && fabsf(rel.y) < ac.size.y && fabsf(rel.z) < ac.size.z) {
+        add.x = __fadd_rn(add.x, __fmul_rn(ac.acc.x, dt));
+        add.y = __fadd_rn(add.y, __fmul_rn(ac.acc.y, dt));
+        add.z = __fadd_rn(add.z, __fmul_rn(ac.acc.z, dt));
+      }
+    } else if (ac.type == SPH_ACC_CYLY) {
+      const float r = len2(__fdiv_rn(rel.x, ac.size.x), __fdiv_rn(rel.z, ac.size.z));
+      if (fabsf(rel.y) < ac.size.y && r < 1.f) {
+        add.x = __fadd_rn(add.x, __fmul_rn(ac.acc.x, dt));
+        add.y = __fadd_rn(add.y, __fmul_rn(ac.acc.y, dt));
+        add.z = __fadd_rn(add.z, __fmul_rn(ac.acc.z, dt));
+      }
+    } else if (ac.type == SPH_ACC_CYLYSM) {
+      const float r = len2(rel.x, rel.z);
+      if (fabsf(rel.y) < ac.size.y && r < ac.size.x) {
+        const float w = __fsub_rn(1.f, __fdiv_rn(r, ac.size.z));
+        add.x = __fadd_rn(add.x, __fmul_rn(__fmul_rn(ac.acc.x, w), dt));
+        add.y = __fadd_rn(add.y, __fmul_rn(__fmul_rn(ac.acc.y, w), dt));
+        add.z = __fadd_rn(add.z, __fmul_rn(__fmul_rn(ac.acc.z, w), dt));
+      }
+    }
+  }
+  return add;
+}
+
+// Colour and dye of computeForceD (System.cu:405-546).  Returns false when
+// nothing is written (CLR_None, or CLR_Vel whose foam estimate is not built).
+__device__ inline bool color_dye(const SimParams& p, float4 xi, float4 vi, float dens, float3 add,
+                                 float* dye, float4& clr) {
+  float cx = 0.2f, cy = 0.5f, cz = 1.f, intens = 0.f;
+  const float dt = p.timeStep;
+  switch (p.clrType) {
+    case SPH_CLR_VELACC: {
+      const float v = __fmul_rn(2.5f, len3(f3(vi.x, vi.y, vi.z)));
+      const float f = __fdiv_rn(__fmul_rn(0.02f, len3(add)), dt);
+      const float clrV = __fadd_rn(p.brightness, __fmul_rn(p.contrast, v));
+      const float clrF = __fmul_rn(p.contrast, f);
+      cx = __fadd_rn(__fmul_rn(cx, clrV), __fmul_rn(0.7f, clrF));
+      cy = __fadd_rn(__fmul_rn(cy, clrV), __fmul_rn(0.35f, clrF));
+      cz = __fadd_rn(__fmul_rn(cz, clrV), __fmul_rn(0.f, clrF));
+    } break;
+    case SPH_CLR_DENSACC: {
+      const float d = __fdiv_rn(__fmul_rn(4.f, __fsub_rn(dens, p.restDensity)), p.restDensity);
+      const float f = __fdiv_rn(__fmul_rn(0.02f, len3(add)), dt);
+      const float clrD = __fadd_rn(p.brightness, __fmul_rn(p.contrast, d));
+      const float clrF = __fmul_rn(p.contrast, f);
+      cx = __fadd_rn(__fmul_rn(cx, clrD), __fmul_rn(0.7f, clrF));
+      cy = __fadd_rn(__fmul_rn(cy, clrD), __fmul_rn(0.7f, clrF));
+      cz = __fadd_rn(__fmul_rn(cz, clrD), __fmul_rn(0.f, clrF));
+    } break;
+    case SPH_CLR_VELRGB: {
+      const float s = __fmul_rn(p.contrast, 2.5f);
+      cx = __fadd_rn(0.5f, __fmul_rn(s, vi.x));
+      cy = __fadd_rn(0.5f, __fmul_rn(s, vi.y));
+      cz = __fadd_rn(0.5f, __fmul_rn(s, vi.z));
+    } break;
+    case SPH_CLR_ACCEL: {
+      const float f = __fdiv_rn(__fmul_rn(0.02f, len3(add)), dt);
+      const float clrF = __fadd_rn(p.brightness, __fmul_rn(p.contrast, f));
+      intens = clrF;
+      cx = __fmul_rn(cx, clrF);
+      cy = __fmul_rn(cy, clrF);
+      cz = __fmul_rn(cz, clrF);
+    } break;
+    case SPH_CLR_DENS: {
+      const float d = __fdiv_rn(__fmul_rn(4.f, __fsub_rn(dens, p.restDensity)), p.restDensity);
+      const float clrD = __fadd_rn(p.brightness, __fmul_rn(p.contrast, d));
+      intens = clrD;
+      cx = __fmul_rn(cx, clrD);
+      cy = __fmul_rn(cy, clrD);
+      cz = __fmul_rn(cz, clrD);
+    } break;
+    default:
+      return false;
+  }
+  if (p.iHue == 1) {
+    cx = intens;
+    cy = 0.f;
+  }
+  if (dye) {
+    if (p.dyeClear > 0) {
+      *dye = 0.f;
+    } else if (p.dyeType > 0) {
+      float dyeCl = *dye;
+      const float rx = __fsub_rn(xi.x, p.dyePos.x), ry = __fsub_rn(xi.y, p.dyePos.y),
+                  rz = __fsub_rn(xi.z, p.dyePos.z);
+      if (p.dyeType == 1) {
+        if (fabsf(rx) < p.dyeSize.x && fabsf(ry) < p.dyeSize.y && fabsf(rz) < p.dyeSize.z) dyeCl = 1.f;
+      } else if (p.dyeType == 2) {
+        if (len3(f3(rx, ry, rz)) < p.dyeSize.y) dyeCl = 1.f;
+      }
+      dyeCl = __fsub_rn(dyeCl, __fmul_rn(dt, p.dyeFade));
+      if (dyeCl < 0.f) dyeCl = 0.f;
+      if (dyeCl >= 0.f) *dye = dyeCl;
+      if (p.iHue == 0) {
+        cx = __fadd_rn(cx, __fmul_rn(0.9f, dyeCl));
+        cy = __fadd_rn(cy, __fmul_rn(0.9f, dyeCl));
+        cz = __fadd_rn(cz, __fmul_rn(1.f, dyeCl));
+      } else {
+        cy = dyeCl;
+      }
+    }
+  }
+  clr = make_float4(cx, cy, cz, 1.f);
+  return true;
+}
+
+}  // namespace sph

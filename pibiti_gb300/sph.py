@@ -1,0 +1,253 @@
+"""Host API: scenes, the SPH system (the cSPH replacement) and the stage
+entry points, over the C ABI.
+
+``SPH`` mirrors the reference's ``cSPH`` (source/SPH/SPH.h:9-50): scenes from
+a Scenes.xml file, ``reset`` / ``drop``-style initial states, ``set_array`` /
+``get_array`` and ``update``.  Arrays are numpy arrays (host memory) or torch
+CUDA tensors (device memory, passed by pointer, no copy through the host).
+``stage`` exposes the reference's per-stage wrappers for code that drives
+the stages itself.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Iterable, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import ARRAY_POS, ARRAY_VEL, SceneInfo, check, lib
+from .params import SimParams
+
+__all__ = ["Scene", "SPH", "ARRAY_POS", "ARRAY_VEL", "stage"]
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _buf(x, dtype=np.float32, cols=4):
+    """(pointer, on_device, keepalive) for a numpy array or torch tensor."""
+    if _is_torch(x):
+        if not x.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return ctypes.c_void_p(x.data_ptr()), bool(x.is_cuda), x
+    a = np.ascontiguousarray(x, dtype=dtype)
+    if cols:
+        a = a.reshape(-1, cols)
+    return ctypes.c_void_p(a.ctypes.data), False, a
+
+
+class Scene:
+    """One scene: SimParams plus the init data Scene keeps beside it."""
+
+    def __init__(self, params: SimParams, info: SceneInfo):
+        self.params = params
+        self.info = info
+
+    @property
+    def title(self) -> str:
+        return self.info.title.decode(errors="replace")
+
+    @classmethod
+    def default(cls) -> "Scene":
+        p, i = SimParams(), SceneInfo()
+        check(lib().sph_scene_default(ctypes.byref(p), ctypes.byref(i)))
+        return cls(p, i)
+
+    @classmethod
+    def parse(cls, xml: str) -> "Scene":
+        p, i = SimParams(), SceneInfo()
+        check(lib().sph_scene_parse(xml.encode(), ctypes.byref(p), ctypes.byref(i)))
+        return cls(p, i)
+
+    @classmethod
+    def load(cls, path: str, index: int) -> "Scene":
+        p, i = SimParams(), SceneInfo()
+        check(lib().sph_scene_load(path.encode(), index, ctypes.byref(p), ctypes.byref(i)))
+        return cls(p, i)
+
+    @staticmethod
+    def count(path: str) -> int:
+        n = ctypes.c_int()
+        check(lib().sph_scene_count(path.encode(), ctypes.byref(n)))
+        return n.value
+
+    @staticmethod
+    def load_all(path: str) -> list["Scene"]:
+        """cSPH::LoadScenes (SPH_Scenes.cpp:171-202)."""
+        return [Scene.load(path, i) for i in range(Scene.count(path))]
+
+    @staticmethod
+    def default_index(path: str) -> int:
+        n = ctypes.c_int()
+        check(lib().sph_scene_default_index(path.encode(), ctypes.byref(n)))
+        return n.value
+
+    def reset(self, kind: int = 0, seed: int = 42):
+        """cSPH::Reset (SPH_Init.cpp:23-79): (pos, vel) float32 (N, 4)."""
+        n = self.params.numParticles
+        pos = np.zeros((n, 4), np.float32)
+        vel = np.zeros((n, 4), np.float32)
+        placed = ctypes.c_uint32()
+        check(lib().sph_scene_reset(ctypes.byref(self.params), ctypes.byref(self.info), kind, seed,
+                                    ctypes.c_void_p(pos.ctypes.data),
+                                    ctypes.c_void_p(vel.ctypes.data), ctypes.byref(placed)))
+        return pos, vel
+
+
+class SPH:
+    """The system handle: one scene, or many independent scenes stepped
+    together (``SPH([p1, p2, ...])``)."""
+
+    def __init__(self, params, stream=None):
+        L = lib()
+        self._h = ctypes.c_void_p()
+        if isinstance(params, SimParams):
+            plist = [params]
+        else:
+            plist = list(params)
+        arr = (SimParams * len(plist))(*plist)
+        if len(plist) == 1:
+            check(L.sph_create(arr, ctypes.byref(self._h)))
+        else:
+            check(L.sph_create_ensemble(arr, len(plist), ctypes.byref(self._h)))
+        self.num_scenes = L.sph_num_scenes(self._h)
+        self.n = L.sph_num_particles(self._h)
+        self.num_cells = L.sph_num_cells(self._h)
+        self.offsets = [L.sph_scene_offset(self._h, i) for i in range(self.num_scenes + 1)]
+        if stream is not None:
+            self.set_stream(stream)
+
+    def close(self) -> None:
+        if self._h:
+            check(lib().sph_destroy(self._h))
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream) -> None:
+        """A torch.cuda.Stream, a raw cudaStream_t int, or None."""
+        handle = getattr(stream, "cuda_stream", stream)
+        check(lib().sph_set_stream(self._h, ctypes.c_void_p(handle or 0)))
+
+    def params(self, scene: int = 0) -> SimParams:
+        p = SimParams()
+        check(lib().sph_get_params(self._h, scene, ctypes.byref(p)))
+        return p
+
+    def set_params(self, p: SimParams, scene: int = 0) -> None:
+        check(lib().sph_set_params(self._h, scene, ctypes.byref(p)))
+
+    def set_array(self, which: int, data, start: int = 0) -> None:
+        """setArray (SPH_Util.cpp:59-71): float4 records from `start`."""
+        ptr, dev, keep = _buf(data)
+        count = keep.shape[0] if not dev else keep.numel() // 4
+        check(lib().sph_set_array(self._h, which, ptr, start, count, int(dev)))
+
+    def get_array(self, which: int, out=None):
+        """getArray (SPH_Util.cpp:44-56): all particles, original order."""
+        if out is None:
+            out = np.empty((self.n, 4), np.float32)
+        ptr, dev, keep = _buf(out)
+        check(lib().sph_get_array(self._h, which, ptr, int(dev)))
+        return out
+
+    def update(self, steps: int = 1) -> None:
+        """cSPH::Update (SPH_Update.cpp:12-81), `steps` times."""
+        check(lib().sph_step(self._h, steps))
+
+    STAGES = ("integrate_count", "scan", "scatter_ids", "place", "density", "force")
+
+    def step_timed(self) -> dict:
+        """One step with per-stage CUDA-event times (ms) on the handle's stream."""
+        out = (ctypes.c_float * len(self.STAGES))()
+        check(lib().sph_step_timed(self._h, out, len(self.STAGES)))
+        return dict(zip(self.STAGES, list(out)))
+
+    def cells(self):
+        """(sortedHash (N,2) uint32, cellStart (C,), cellEnd (C,)) of the last step."""
+        h = np.empty((self.n, 2), np.uint32)
+        cs = np.empty(self.num_cells, np.uint32)
+        ce = np.empty(self.num_cells, np.uint32)
+        check(lib().sph_get_cells(self._h, ctypes.c_void_p(h.ctypes.data),
+                                  ctypes.c_void_p(cs.ctypes.data), ctypes.c_void_p(ce.ctypes.data), 0))
+        return h, cs, ce
+
+    def fields(self):
+        """(density, pressure) of the last step, sorted order."""
+        d = np.empty(self.n, np.float32)
+        p = np.empty(self.n, np.float32)
+        check(lib().sph_get_fields(self._h, ctypes.c_void_p(d.ctypes.data),
+                                   ctypes.c_void_p(p.ctypes.data), 0))
+        return d, p
+
+    def stats(self) -> np.ndarray:
+        """(scenes, 4) doubles: KE, mean density, max |rho/rho0-1|, non-finite count."""
+        out = (ctypes.c_double * (4 * self.num_scenes))()
+        check(lib().sph_stats(self._h, out))
+        return np.array(out, dtype=np.float64).reshape(self.num_scenes, 4)
+
+    def flags(self) -> int:
+        f = ctypes.c_uint32()
+        check(lib().sph_flags(self._h, ctypes.byref(f)))
+        return f.value
+
+
+class _Stage:
+    """The reference's per-stage wrappers (System.cuh, radixsort.cuh) over
+    device pointers (torch CUDA tensors)."""
+
+    @staticmethod
+    def _p(t):
+        if t is None:
+            return ctypes.c_void_p(0)
+        if not (_is_torch(t) and t.is_cuda):
+            raise TypeError("stage entry points take CUDA tensors")
+        return ctypes.c_void_p(t.data_ptr())
+
+    def set_parameters(self, p: SimParams) -> None:
+        check(lib().sph_setParameters(ctypes.byref(p)))
+
+    def set_stream(self, stream) -> None:
+        handle = getattr(stream, "cuda_stream", stream)
+        check(lib().sph_setStageStream(ctypes.c_void_p(handle or 0)))
+
+    def integrate(self, old_pos, new_pos, old_vel, new_vel, n: int) -> None:
+        P = self._p
+        check(lib().sph_integrate(P(old_pos), P(new_pos), P(old_vel), P(new_vel), n))
+
+    def calc_hash(self, pos, particle_hash, n: int) -> None:
+        check(lib().sph_calcHash(self._p(pos), self._p(particle_hash), n))
+
+    def radix_sort(self, d0, d1, n: int, bits: int) -> None:
+        check(lib().sph_RadixSort(self._p(d0), self._p(d1), n, bits))
+
+    def reorder(self, old_pos, old_vel, sorted_pos, sorted_vel, particle_hash, cell_start,
+                n: int, num_cells: int) -> None:
+        P = self._p
+        check(lib().sph_reorder(P(old_pos), P(old_vel), P(sorted_pos), P(sorted_vel),
+                                P(particle_hash), P(cell_start), n, num_cells))
+
+    def collide(self, sorted_pos, sorted_vel, new_vel, pressure, density, particle_hash,
+                cell_start, n: int, num_cells: int, clr=None, dye=None) -> None:
+        P = self._p
+        check(lib().sph_collide(None, None, P(clr), P(sorted_pos), P(sorted_vel), None,
+                                P(new_vel), P(pressure), P(density), P(dye), P(particle_hash),
+                                P(cell_start), n, num_cells))
+
+    def sync(self) -> None:
+        check(lib().sph_threadSync())
+
+
+stage = _Stage()

@@ -1,0 +1,180 @@
+"""GPU parity of the fused system step (sph_step) through the C ABI.
+
+Against the golden fixtures (the reference's own kernels): sorted hash,
+cellStart and integrated positions bit-exact; density within DENS_RTOL;
+velocities within the force tolerance of test_gpu_stage.  Against the
+oracle: multi-step trajectories, the ensemble, and size-independent
+properties at the 1,048,576-particle workload.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import params_from
+from pibiti_gb300 import configs
+from pibiti_gb300.sph import ARRAY_POS, ARRAY_VEL, SPH, Scene
+
+pytestmark = pytest.mark.gpu
+
+DENS_RTOL = 1e-5
+CASES = ["dambreak", "truncate", "features", "bigrid", "tiny"]
+
+
+def system_from(p, pos, vel):
+    s = SPH(p)
+    s.set_array(ARRAY_POS, pos)
+    s.set_array(ARRAY_VEL, vel)
+    return s
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_step_vs_reference(cuda, golden, case):
+    g = golden(f"step_{case}.npz")
+    p = params_from(g["params"])
+    with system_from(p, g["pos_in"], g["vel_in"]) as s:
+        s.update(1)
+        pos, vel = s.get_array(ARRAY_POS), s.get_array(ARRAY_VEL)
+        sh, cs, ce = s.cells()
+        dens, pres = s.fields()
+        flags = s.flags()
+    np.testing.assert_array_equal(sh, g["sorted"])
+    np.testing.assert_array_equal(cs, g["cell_start"])
+    cnt = np.bincount(g["sorted"][:, 0], minlength=p.numCells)
+    np.testing.assert_array_equal(ce[cnt > 0], g["cell_start"][cnt > 0] + cnt[cnt > 0])
+    assert np.all(ce[cnt == 0] == 0xFFFFFFFF)
+    np.testing.assert_array_equal(pos, g["pos"])
+    d64, _ = oracle.density(p, g["sorted_pos"], g["sorted"], g["cell_start"], fp64=True)
+    np.testing.assert_allclose(dens, d64, rtol=DENS_RTOL, atol=1e-2)
+    np.testing.assert_allclose(dens, g["density"], rtol=DENS_RTOL, atol=1e-2)
+    from test_gpu_stage import check_force
+    check_force(p, g["sorted"], g["sorted_pos"], g["sorted_vel"], dens, pres, g["cell_start"], vel)
+    # truncation is reported (bit 0) exactly when a cell overflowed
+    overflow = cnt.max() > p.maxParInCell
+    assert bool(flags & 1) == overflow
+
+
+def test_multistep_matches_oracle(cuda):
+    """100 steps of the 4,096-particle dam break: the fused GPU step and the
+    single-precision oracle perform the same IEEE operations."""
+    w = configs.dambreak_small(side=16)
+    p = Scene.parse(w.xml).params
+    with system_from(p, w.pos, w.vel) as s:
+        s.update(100)  # graph-replayed pairs of steps
+        pos, vel = s.get_array(ARRAY_POS), s.get_array(ARRAY_VEL)
+    opos, ovel = oracle.step(p, w.pos, w.vel, steps=100)
+    np.testing.assert_array_equal(pos, opos)
+    np.testing.assert_array_equal(vel, ovel)
+
+
+def test_drift_bounds(cuda):
+    """Kinetic energy and mean density of GPU vs oracle trajectories, 300
+    steps of the 32,768-particle dam break: within 1e-4 relative."""
+    w = configs.dambreak_small(side=32)
+    p = Scene.parse(w.xml).params
+    with system_from(p, w.pos, w.vel) as s:
+        s.update(300)
+        st = s.stats()[0]
+        d_gpu, _ = s.fields()
+    opos, ovel = oracle.step(p, w.pos, w.vel, steps=300)
+    ke_o, _ = oracle.reduce(p, ovel)
+    assert abs(st[0] - ke_o) <= 1e-4 * ke_o
+    assert st[3] == 0
+    assert abs(st[1] - d_gpu.astype(np.float64).mean()) <= 1e-6 * st[1]
+    # k=3 is soft: the 0.73 m column compresses to about twice rest density
+    assert p.restDensity < st[1] < 4 * p.restDensity
+
+
+def test_ensemble_equals_separate_runs(cuda):
+    """Three scenes of different size and parameters in one handle give the
+    same bits as three separate handles."""
+    ws = [configs.dambreak_small(side=s, seed=i) for i, s in enumerate((8, 12, 16))]
+    ps = []
+    for i, w in enumerate(ws):
+        p = Scene.parse(w.xml).params
+        p.stiffness = 1.0 + i
+        p.viscosity = 2.0 + i
+        ps.append(p)
+    with SPH(ps) as e:
+        e.set_array(ARRAY_POS, np.concatenate([w.pos for w in ws]))
+        e.set_array(ARRAY_VEL, np.concatenate([w.vel for w in ws]))
+        e.update(20)
+        epos, evel = e.get_array(ARRAY_POS), e.get_array(ARRAY_VEL)
+        offs = e.offsets
+        sh, cs, ce = e.cells()
+    for k, (w, p) in enumerate(zip(ws, ps)):
+        with system_from(p, w.pos, w.vel) as s:
+            s.update(20)
+            np.testing.assert_array_equal(epos[offs[k]:offs[k + 1]], s.get_array(ARRAY_POS))
+            np.testing.assert_array_equal(evel[offs[k]:offs[k + 1]], s.get_array(ARRAY_VEL))
+            ssh, scs, _ = s.cells()
+            np.testing.assert_array_equal(sh[offs[k]:offs[k + 1]], ssh)
+
+
+def test_set_get_roundtrip(cuda):
+    torch = cuda
+    w = configs.dambreak_small(side=10)
+    p = Scene.parse(w.xml).params
+    with system_from(p, w.pos, w.vel) as s:
+        np.testing.assert_array_equal(s.get_array(ARRAY_POS), w.pos)
+        s.update(3)
+        # partial write in original indices after the state has been permuted
+        new = np.full((17, 4), 0.5, np.float32)
+        s.set_array(ARRAY_VEL, new, start=100)
+        v = s.get_array(ARRAY_VEL)
+        np.testing.assert_array_equal(v[100:117], new)
+        # device-to-device through torch tensors
+        t = torch.empty((s.n, 4), dtype=torch.float32, device="cuda")
+        s.get_array(ARRAY_POS, out=t)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(t.cpu().numpy(), s.get_array(ARRAY_POS))
+
+
+def test_nan_is_flagged(cuda):
+    w = configs.dambreak_small(side=8)
+    p = Scene.parse(w.xml).params
+    pos = w.pos.copy()
+    pos[5, 1] = np.nan
+    with system_from(p, pos, w.vel) as s:
+        s.update(1)
+        assert s.flags() & 2
+        assert s.stats()[0][3] > 0
+
+
+def test_grid_too_small_rejected(cuda):
+    from pibiti_gb300 import _lib
+    xml = configs.scene_xml(**configs.dambreak_attrs(64, (0, 0, 0), (0.1, 1.0, 1.0)))
+    p = Scene.parse(xml).params
+    with pytest.raises(_lib.SphError) as e:
+        SPH(p)
+    assert e.value.code == 3
+
+
+def test_million_particle_properties(cuda):
+    """The 1,048,576-particle double dam break: after 20 steps the neighbour
+    structures are a stable sort of (hash, original index), cell ranges
+    partition the particles, and density matches the double-precision
+    oracle on the GPU's own sorted positions."""
+    w = configs.dambreak_double(steps=20)
+    p = Scene.parse(w.xml).params
+    with system_from(p, w.pos, w.vel) as s:
+        s.update(20)
+        sh, cs, ce = s.cells()
+        dens, _ = s.fields()
+        pos = s.get_array(ARRAY_POS)
+    n = len(w.pos)
+    keys, ids = sh[:, 0].astype(np.int64), sh[:, 1].astype(np.int64)
+    assert np.all(np.diff(keys) >= 0)
+    same = np.diff(keys) == 0
+    assert np.all(np.diff(ids)[same] > 0)
+    assert np.array_equal(np.sort(ids), np.arange(n))
+    cnt = np.bincount(keys, minlength=p.numCells)
+    nz = cnt > 0
+    starts = np.concatenate([[0], np.cumsum(cnt)[:-1]])
+    np.testing.assert_array_equal(cs[nz], starts[nz])
+    np.testing.assert_array_equal(ce[nz], starts[nz] + cnt[nz])
+    # hashes are the hashes of the sorted positions
+    spos = pos[ids]
+    np.testing.assert_array_equal(oracle.calc_hash(p, spos)[:, 0], sh[:, 0])
+    kv = np.stack([sh[:, 0], ids.astype(np.uint32)], axis=1)
+    d64, _ = oracle.density(p, spos, kv, cs, fp64=True)
+    np.testing.assert_allclose(dens, d64, rtol=DENS_RTOL, atol=1e-2)
