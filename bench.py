@@ -67,19 +67,16 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
-    summary (profiles/), scaled to this workload there; None if absent."""
-    path = os.path.join(ROOT, "profiles", "force_double_dambreak_1M.md")
+def ncu_traffic(kernel: str):
+    """Per-launch DRAM bytes (read + write) of `kernel` from the committed ncu
+    summary of this workload (profiles/); None if it has no entry."""
+    path = os.path.join(ROOT, "profiles", "walk_kernels_double_dambreak_1M.md")
     if not os.path.exists(path):
-        return None, None
-    kernel, val = None, None
+        return None
     for line in open(path):
-        if line.startswith("traffic_bytes_per_launch:"):
-            val = float(line.split(":")[1].split()[0])
-        if line.startswith("kernel:"):
-            kernel = line.split(":", 1)[1].strip()
-    return kernel, val
+        if line.startswith(f"traffic {kernel}:"):
+            return float(line.split(":")[1].split()[0])
+    return None
 
 
 class ClockSampler:
@@ -297,7 +294,7 @@ def main():
     alg = bp * n + bc * p.numCells
     peak, peak_kind = measured_peaks()
     achieved = alg / (stage_ms[dom] / 1e3) / 1e9
-    kname, traffic = ncu_traffic()
+    traffic = ncu_traffic(f"k_{dom}")
     roofline = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                 "algorithmic_bytes": alg, "peak_source": peak_kind,
