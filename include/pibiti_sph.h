@@ -88,6 +88,17 @@ int sph_calcHash(const sph_float4* pos, sph_uint2* particleHash, int numParticle
    after an odd number it is in pData1, exactly as with the reference. */
 int sph_RadixSort(sph_uint2* pData0, sph_uint2* pData1, uint32_t elements, uint32_t bits);
 
+/* The same sort without any device allocation; it has no counterpart in the
+   reference.  For callers that must not call cudaMalloc/cudaFree while they
+   run (a frame loop that cannot absorb cudaFree's device-wide wait, or a
+   process whose device memory is held by another allocator).  Its scratch
+   is a 2.0 MiB array inside the library that every GPU loading it keeps
+   until exit, so at most 4,194,304 pairs (larger: SPH_ERR_ARG).  The first
+   call on a device looks up the array's address, so make it before any
+   stream capture; calls that overlap on the GPU share the array and race.
+   Runs on the stage stream; result location as sph_RadixSort. */
+int sph_RadixSort_noalloc(sph_uint2* pData0, sph_uint2* pData1, uint32_t elements, uint32_t bits);
+
 /* reorder (System.cuh:29-30): cellStart[c] = first sorted index of cell c
    (0xFFFFFFFF when empty), pos/vel gathered into sorted order. */
 int sph_reorder(const sph_float4* oldPos, const sph_float4* oldVel, sph_float4* sortedPos,

@@ -53,6 +53,7 @@ SIGNATURES = {
     "sph_integrate": [vp, vp, vp, vp, i32],
     "sph_calcHash": [vp, vp, i32],
     "sph_RadixSort": [vp, vp, u32, u32],
+    "sph_RadixSort_noalloc": [vp, vp, u32, u32],
     "sph_reorder": [vp, vp, vp, vp, vp, vp, u32, u32],
     "sph_collide": [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, u32, u32],
     "sph_create": [P(SimParams), P(vp)],

@@ -36,6 +36,8 @@ int fail(int code, const char* fmt, ...) {
   return code;
 }
 
+cudaStream_t stage_stream() { return g_stage_stream; }
+
 int cuda_check(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return SPH_OK;
   return fail(e == cudaErrorMemoryAllocation ? SPH_ERR_NOMEM : SPH_ERR_CUDA, "%s: %s (%s)", what,
