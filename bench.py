@@ -185,6 +185,78 @@ def run_reference(args):
     return 0
 
 
+def run_ensemble(args):
+    """256 independent dam-break scenes (4k-64k particles, k in [1,5], mu in
+    [1,6]) stepped together in one handle: `steps` steps captured as one CUDA
+    graph and launched once, after the autotuner picked the walk shape.  The
+    same scenes stepped one handle at a time (first 32 scenes) are timed for
+    comparison."""
+    import torch
+    from pibiti_gb300 import configs
+    from pibiti_gb300.sph import ARRAY_POS, ARRAY_VEL, SPH, Scene
+    torch.cuda.set_device(0)
+    e = configs.ensemble(steps=args.steps)
+    ps = [Scene.parse(x).params for x in e.xmls]
+    stream = torch.cuda.Stream()
+    sysm = SPH(ps, stream=stream)
+    sysm.set_array(ARRAY_POS, e.pos)
+    sysm.set_array(ARRAY_VEL, e.vel)
+    sysm.update(args.warmup)
+    chosen, tune_ms = sysm.autotune(trial_steps=5)
+    steps = args.steps + (args.steps % 2)
+    sysm.set_graph_steps(steps)
+    sysm.update(steps)  # builds and runs the graph once (untimed)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sysm.update(steps)  # one graph launch
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    value = sysm.n * steps / (ms / 1e3)
+    st = sysm.stats()
+    sysm.close()
+    # the same scenes, one handle each, for the first 32 scenes
+    sub = 32
+    t_sep, n_sep = 0.0, 0
+    off = 0
+    for k in range(sub):
+        n = e.sizes[k]
+        with SPH(ps[k], stream=stream) as one:
+            one.set_array(ARRAY_POS, e.pos[off:off + n])
+            one.set_array(ARRAY_VEL, e.vel[off:off + n])
+            one.update(4)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            one.update(50)
+            b.record(stream)
+            torch.cuda.synchronize()
+            t_sep += a.elapsed_time(b) / 1e3
+            n_sep += n * 50
+        off += n
+    line = {
+        "metric": "ensemble particle-steps/s", "value": value, "unit": UNIT,
+        "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched ensemble: {len(ps)} dam-break scenes, "
+                               f"{min(e.sizes)}-{max(e.sizes)} particles (log-uniform, x512), "
+                               f"k in [1,5], mu in [1,6]", "particles": e.n,
+                   "cells": int(sum(p.numCells for p in ps)),
+                   "graph": f"{steps} steps captured as one CUDA graph, one launch"},
+        "autotune": {"chosen_threads": SPH.WALK_THREADS[chosen], "ms_per_step": tune_ms},
+        "separate_handles": {"scenes": sub, "value": n_sep / t_sep, "unit": UNIT},
+        "clocks": clk,
+        "state_check": {"max_density_dev": float(st[:, 2].max()), "nonfinite": float(st[:, 3].sum())},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def workload_config(p, n=None):
     cfg = {"workload": "double dam break, 1,048,576 particles: two 64x128x64 lattices at "
                        "spacing 0.5h (h=0.0457 m) in a 6.0x3.4x1.7 m box, +-1% jitter, "
@@ -205,11 +277,15 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--warm-steps", type=int, default=200)
+    ap.add_argument("--workload", choices=["double_dambreak", "ensemble"], default="double_dambreak",
+                    help="ensemble: the 256-scene batched ensemble (a separate measurement)")
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "ensemble":
+        return run_ensemble(args)
 
     import numpy as np
     import torch

@@ -159,6 +159,22 @@ int sph_get_array(SphSystem* sys, uint32_t which, sph_float4* out, int dst_on_de
    CUDA graph. */
 int sph_step(SphSystem* sys, uint32_t steps);
 
+/* Steps captured per CUDA graph (even, >= 2; default 2).  sph_step(sys, k)
+   replays floor(k / steps_per_graph) graph launches and runs the rest
+   directly, so a whole run of steps_per_graph steps is one launch. */
+int sph_set_graph_steps(SphSystem* sys, uint32_t steps_per_graph);
+
+/* Launch shape of the density and force walks: 0 = 64 threads per block,
+   1 = 128 (default), 2 = 256, each compiled for full occupancy at that size. */
+int sph_set_walk_shape(SphSystem* sys, uint32_t shape);
+int sph_get_walk_shape(SphSystem* sys, uint32_t* shape, uint32_t* threads_per_block);
+
+/* Autotuner: times `trial_steps` steps with each walk shape on this
+   handle's own scenes and keeps the fastest (written to *chosen; per-shape
+   ms per step to ms_per_step[3] if not NULL).  The particle state is saved
+   before and restored after, so tuning does not advance the simulation. */
+int sph_autotune(SphSystem* sys, uint32_t trial_steps, float* ms_per_step, uint32_t* chosen);
+
 /* One step with a CUDA event recorded on the handle's stream before the
    first stage and after each of the six stages (1: integrate + cell count,
    2: scan, 3: id scatter, 4: stable placement, 5: density, 6: force);

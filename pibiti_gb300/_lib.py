@@ -69,6 +69,10 @@ SIGNATURES = {
     "sph_get_array": [vp, u32, vp, i32],
     "sph_step": [vp, u32],
     "sph_step_timed": [vp, P(ctypes.c_float), u32],
+    "sph_set_graph_steps": [vp, u32],
+    "sph_set_walk_shape": [vp, u32],
+    "sph_get_walk_shape": [vp, P(u32), P(u32)],
+    "sph_autotune": [vp, u32, P(ctypes.c_float), P(u32)],
     "sph_get_cells": [vp, vp, vp, vp, i32],
     "sph_get_fields": [vp, vp, vp, i32],
     "sph_num_cells": [vp],

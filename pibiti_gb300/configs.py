@@ -136,3 +136,48 @@ def uniform_stress(n: int = 16_777_216, seed: int = 42, steps: int = 200,
     xml = scene_xml(**dambreak_attrs(n, (0.0, 0.0, 0.0), tuple(box), h=h, spacing=spacing))
     return Workload(f"uniform_{n}", xml, pos, np.zeros_like(pos), steps,
                     dict(box=tuple(box), h=h, spacing=spacing))
+
+
+@dataclass
+class Ensemble:
+    name: str
+    xmls: list
+    pos: np.ndarray  # all scenes concatenated, scene order
+    vel: np.ndarray
+    sizes: list
+    steps: int
+    notes: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return len(self.pos)
+
+
+def ensemble(scenes: int = 256, nmin: int = 4096, nmax: int = 65536, seed: int = 42,
+             steps: int = 500) -> Ensemble:
+    """Independent dam-break scenes for the batched ensemble: particle counts
+    log-uniform in [nmin, nmax] rounded to 512, stiffness k ~ U[1, 5] and
+    viscosity mu ~ U[1, 6] per scene, same h, spacing and dt.  Each scene is a
+    16 x 16 (n <= 16384) or 32 x 32 based column filled layer by layer from
+    the low corner of a box three columns wide."""
+    rng = np.random.default_rng(seed)
+    r = particle_radius(SPACING)
+    o = _inset(r)
+    xmls, pos, sizes = [], [], []
+    for s in range(scenes):
+        n = int(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))
+        n = max(512, (n + 256) // 512 * 512)
+        base = 16 if n <= 16384 else 32
+        layers = -(-n // (base * base))
+        block = lattice((base, layers, base), (o, o + r, o), SPACING, rng)[:n]
+        width = (base - 1) * SPACING + 2 * o
+        box = (3.0 * width, (layers - 1) * SPACING * 1.25 + 2 * o + 0.1, width + 0.02)
+        k = float(rng.uniform(1.0, 5.0))
+        mu = float(rng.uniform(1.0, 6.0))
+        xmls.append(scene_xml(**dambreak_attrs(n, (0.0, 0.0, 0.0), box, stiffness=k,
+                                               viscosity=mu)))
+        pos.append(block)
+        sizes.append(n)
+    pos = np.concatenate(pos)
+    return Ensemble(f"ensemble_{scenes}", xmls, pos, np.zeros_like(pos), sizes, steps,
+                    dict(total=int(pos.shape[0])))

@@ -33,16 +33,17 @@ def nvcc() -> str:
     return cand
 
 
-def _flags(verbose_ptxas: bool):
+def _flags(verbose_ptxas: bool, defines=()):
     f = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
          "-I", os.path.join(ROOT, "include"), "-I", HERE]
+    f += [f"-D{d}" for d in defines]
     if verbose_ptxas:
         f += ["-Xptxas", "-v"]
     return f
 
 
-def _compile(src: str, obj: str, cuda: bool, verbose_ptxas: bool) -> str:
-    cmd = [nvcc(), "-c", os.path.join(HERE, src), "-o", obj] + _flags(verbose_ptxas)
+def _compile(src: str, obj: str, cuda: bool, verbose_ptxas: bool, defines=()) -> str:
+    cmd = [nvcc(), "-c", os.path.join(HERE, src), "-o", obj] + _flags(verbose_ptxas, defines)
     if cuda:
         cmd += ARCH
     else:
@@ -64,29 +65,32 @@ def _stale() -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force: bool = False, verbose_ptxas: bool = False) -> str:
-    if not force and not _stale():
+def build(force: bool = False, verbose_ptxas: bool = False, defines=(), out: str = None) -> str:
+    """Build the library; `defines` (NAME=VALUE strings) and `out` (another
+    library path) build a variant, e.g. another launch shape for the walks."""
+    lib = out or LIB
+    if not force and out is None and not defines and not _stale():
         return LIB
-    os.makedirs(OUT_DIR, exist_ok=True)
-    objdir = os.path.join(OUT_DIR, "obj")
+    os.makedirs(os.path.dirname(lib), exist_ok=True)
+    objdir = lib + ".obj"
     os.makedirs(objdir, exist_ok=True)
     jobs = [(s, os.path.join(objdir, s + ".o"), True) for s in CUDA_SOURCES]
     jobs += [(s, os.path.join(objdir, s + ".o"), False) for s in HOST_SOURCES]
     logs = {}
     with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
-        futs = {ex.submit(_compile, s, o, c, verbose_ptxas): s for s, o, c in jobs}
+        futs = {ex.submit(_compile, s, o, c, verbose_ptxas, defines): s for s, o, c in jobs}
         for f in cf.as_completed(futs):
             logs[futs[f]] = f.result()
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc(), "-shared", "-o", tmp] + [o for _, o, _ in jobs] + ARCH + ["-lcuda"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if verbose_ptxas:
         for s, log in sorted(logs.items()):
             sys.stderr.write(f"== {s}\n{log}")
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":

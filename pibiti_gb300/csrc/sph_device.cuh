@@ -233,9 +233,12 @@ __device__ __forceinline__ float density_pair(float4 a, float4 b, float h2, floa
   return acc;
 }
 
-// Constants of compForcePair hoisted out of the neighbour loop.
+// Constants of compForcePair hoisted out of the neighbour loop.  h2_out is
+// two ulps above fl(h*h): a squared distance at or above it has a correctly
+// rounded square root >= h, so the pair contributes nothing (r < h fails)
+// and can be skipped before the division and square root.
 struct ForceConsts {
-  float h, minDist, spiky, vterm, minDens;
+  float h, minDist, spiky, vterm, minDens, h2_out;
 };
 __device__ __forceinline__ ForceConsts force_consts(const SimParams& p) {
   ForceConsts k;
@@ -244,8 +247,13 @@ __device__ __forceinline__ ForceConsts force_consts(const SimParams& p) {
   k.spiky = p.SpikyKern;
   k.vterm = __fmul_rn(p.LapKern, p.viscosity);
   k.minDens = p.minDens;
+  k.h2_out = __int_as_float(__float_as_int(__fmul_rn(p.h, p.h)) + 2);
   return k;
 }
+
+__device__ __forceinline__ void force_pair_near(const ForceConsts& k, float4 vi, float di, float pi,
+                                                float4 vj, float dj, float pj, float rx, float ry,
+                                                float rz, float dist2, float3& acc);
 
 // compForceCell inner step + compForcePair (Kernel_Cell.cui:210-228,
 // 251-258): d12 = min(minDens, 1/(rho_i rho_j)); r = max(minDist, |x_i-x_j|);
@@ -253,11 +261,19 @@ __device__ __forceinline__ ForceConsts force_consts(const SimParams& p) {
 __device__ __forceinline__ void force_pair(const ForceConsts& k, float4 xi, float4 vi, float di,
                                            float pi, float4 xj, float4 vj, float dj, float pj,
                                            float3& acc) {
+  const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
+  const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
+  force_pair_near(k, vi, di, pi, vj, dj, pj, rx, ry, rz, dist2, acc);
+}
+
+// The part of force_pair after the squared distance; the fused walk calls it
+// only for candidates not excluded by ForceConsts::h2_out (and for NaN).
+__device__ __forceinline__ void force_pair_near(const ForceConsts& k, float4 vi, float di, float pi,
+                                                float4 vj, float dj, float pj, float rx, float ry,
+                                                float rz, float dist2, float3& acc) {
   const float dd = __fdiv_rn(1.0f, __fmul_rn(di, dj));
   const float d12 = fminf(k.minDens, dd);
-  const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
   const float vx = __fsub_rn(vj.x, vi.x), vy = __fsub_rn(vj.y, vi.y), vz = __fsub_rn(vj.z, vi.z);
-  const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
   const float r = fmaxf(k.minDist, __fsqrt_rn(dist2));
   if (r < k.h) {
     const float c = __fsub_rn(k.h, r);

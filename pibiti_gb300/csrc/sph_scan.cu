@@ -161,7 +161,7 @@ radix_scatter(const uint2* __restrict__ src, uint2* __restrict__ dst, uint32_t n
   constexpr int kWarps = kThreads / 32;
   __shared__ uint32_t base[256];
   __shared__ uint32_t wcnt[kWarps][256];
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int t = threadIdx.x, warp = t >> 5;
   base[t] = offs[(size_t)t * tiles + blockIdx.x];
 #pragma unroll
   for (int w = 0; w < kWarps; ++w) wcnt[w][t] = 0;

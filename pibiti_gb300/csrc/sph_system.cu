@@ -118,31 +118,59 @@ k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   id_out[dest] = me;
 }
 
-// The 27-cell walk of the fused kernels: neighbour cells outside the grid
-// are skipped (validate_params checks that the reference's wrapped cells
-// there cannot hold neighbours), cells are visited z, y, x and each cell's
-// first maxParInCell sorted entries in order, as compDensCell /
-// compForceCell do.  `visit(j)` is called for every candidate j != i;
-// `cell_done()` after each cell.  Returns true if a cell was truncated.
-template <class Visit, class CellDone>
-__device__ __forceinline__ bool walk27(const SceneDesc& d, float4 xi, uint32_t i,
-                                       const uint32_t* __restrict__ start,
-                                       const uint32_t* __restrict__ count, Visit visit,
-                                       CellDone cell_done) {
+// Launch shapes of the two walks: (threads per block, minimum resident
+// blocks per SM) pairs; sph_autotune picks one per handle by timing them on
+// the handle's own scenes.  Shape 1 (128, 4) is the default, the fastest on
+// GB300 for the 1M-particle dam break.
+constexpr int kWalkShapes = 3;
+constexpr int kWalkBlocks[kWalkShapes] = {64, 128, 256};
+constexpr int kDefaultShape = 1;
+
+// Neighbour masks: with 3 * maxParInCell <= 64, the density pass records for
+// each particle and each of the 9 neighbour rows (dz, dy) one 64-bit mask
+// over the row's candidates (the row's up to 3 cells, each truncated at
+// maxParInCell, concatenated in walk order): bit set = squared distance below
+// ForceConsts::h2_out (or NaN).  The force pass visits exactly those
+// candidates, in the same order, so its sums are unchanged, and skips the
+// rest, which the density pass has shown contribute nothing.
+constexpr int kRows = 9;
+constexpr uint32_t kMaskMaxPerCell = 21;
+#ifndef SPH_WALK_MASKS
+#define SPH_WALK_MASKS 1  // 0: no mask buffer (saves 72 B per particle)
+#endif
+
+__device__ __forceinline__ float h2_out_of(const SimParams& p) {
+  return __int_as_float(__float_as_int(__fmul_rn(p.h, p.h)) + 2);
+}
+
+template <bool kMask, int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+k_density(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
+          const float4* __restrict__ pos, const uint32_t* __restrict__ start,
+          const uint32_t* __restrict__ count, float* __restrict__ dens_out,
+          float* __restrict__ pres_out, unsigned long long* __restrict__ masks,
+          uint32_t* __restrict__ flags) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
   const SimParams& p = d.p;
+  const float4 xi = pos[i];
+  const float h2 = p.h2, h2_out = h2_out_of(p);
   const int3 g = grid_pos(p, xi);
   const int gx = (int)p.gridSize.x, gy = (int)p.gridSize.y, gz = (int)p.gridSize.z;
   const int cx = min(max(g.x, 0), gx - 1), cy = min(max(g.y, 0), gy - 1), cz = min(max(g.z, 0), gz - 1);
   const uint32_t maxpc = p.maxParInCell;
+  const int x0 = max(cx - 1, 0), x1 = min(cx + 1, gx - 1);
+  float sum = 0.f;
   bool trunc = false;
-  for (int dz = -1; dz <= 1; ++dz) {
-    const int z = cz + dz;
-    if (z < 0 || z >= gz) continue;
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int y = cy + dy;
-      if (y < 0 || y >= gy) continue;
+#pragma unroll 1
+  for (int r = 0; r < kRows; ++r) {
+    const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
+    unsigned long long rowmask = 0;
+    if (z >= 0 && z < gz && y >= 0 && y < gy) {
       const uint32_t row = d.c_off + (uint32_t)(z * (int)p.gridSize_yx + y * gx);
-      const int x0 = max(cx - 1, 0), x1 = min(cx + 1, gx - 1);
+      uint32_t bit = 0;
+#pragma unroll 1
       for (int x = x0; x <= x1; ++x) {
         const uint32_t c = row + (uint32_t)x;
         uint32_t n = __ldg(count + c);
@@ -151,66 +179,136 @@ __device__ __forceinline__ bool walk27(const SceneDesc& d, float4 xi, uint32_t i
           n = maxpc;
         }
         const uint32_t s0 = __ldg(start + c);
-        for (uint32_t j = s0; j < s0 + n; ++j)
-          if (j != i) visit(j);
-        cell_done();
+        float cell = 0.f;
+        uint32_t m = 0;
+        auto cand = [&](uint32_t k) {
+          const float4 xj = __ldg(pos + s0 + k);
+          const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
+          const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+          if (r2 < h2) {
+            const float cc = __fsub_rn(h2, r2);
+            cell = __fmaf_rn(__fmul_rn(cc, cc), cc, cell);
+          }
+          if (kMask && !(r2 >= h2_out)) m |= 1u << k;
+        };
+        // only the particle's own cell holds i
+        const uint32_t self = (r == 4 && x == cx) ? i - s0 : 0xffffffffu;
+        if (self < n) {
+#pragma unroll 4
+          for (uint32_t k = 0; k < self; ++k) cand(k);
+#pragma unroll 4
+          for (uint32_t k = self + 1; k < n; ++k) cand(k);
+        } else {
+#pragma unroll 4
+          for (uint32_t k = 0; k < n; ++k) cand(k);
+        }
+        sum = __fadd_rn(sum, cell);
+        if (kMask) rowmask |= (unsigned long long)m << bit;
+        bit += n;
       }
     }
+    if (kMask) masks[(size_t)r * N + i] = rowmask;
   }
-  return trunc;
-}
-
-__global__ void __launch_bounds__(kBlock)
-k_density(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
-          const float4* __restrict__ pos, const uint32_t* __restrict__ start,
-          const uint32_t* __restrict__ count, float* __restrict__ dens_out,
-          float* __restrict__ pres_out, uint32_t* __restrict__ flags) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
-  const float4 xi = pos[i];
-  const float h2 = d.p.h2;
-  float sum = 0.f, cell = 0.f;
-  int nbr = 0;
-  const bool trunc = walk27(
-      d, xi, i, start, count,
-      [&](uint32_t j) { cell = density_pair(xi, __ldg(pos + j), h2, cell, nbr); },
-      [&]() {
-        sum = __fadd_rn(sum, cell);
-        cell = 0.f;
-      });
   if (trunc) atomicOr(flags, 1u);
-  const float dens = __fmul_rn(__fmul_rn(sum, d.p.Poly6Kern), d.p.particleMass);
+  const float dens = __fmul_rn(__fmul_rn(sum, p.Poly6Kern), p.particleMass);
   dens_out[i] = dens;
-  pres_out[i] = __fmul_rn(__fsub_rn(dens, d.p.restDensity), d.p.stiffness);
+  pres_out[i] = __fmul_rn(__fsub_rn(dens, p.restDensity), p.stiffness);
 }
 
-__global__ void __launch_bounds__(kBlock)
+template <bool kMask, int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
 k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
         const float4* __restrict__ pos, const float4* __restrict__ vel,
         const float* __restrict__ dens, const float* __restrict__ pres,
         const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
-        float4* __restrict__ vel_out) {
+        const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
+  const SimParams& p = d.p;
   const float4 xi = pos[i], vi = vel[i];
   const float di = dens[i], pi = pres[i];
-  const ForceConsts k = force_consts(d.p);
-  float3 F = make_float3(0.f, 0.f, 0.f), cell = F;
-  walk27(
-      d, xi, i, start, count,
-      [&](uint32_t j) {
-        force_pair(k, xi, vi, di, pi, __ldg(pos + j), __ldg(vel + j), __ldg(dens + j),
-                   __ldg(pres + j), cell);
-      },
-      [&]() {
-        F.x = __fadd_rn(F.x, cell.x);
-        F.y = __fadd_rn(F.y, cell.y);
-        F.z = __fadd_rn(F.z, cell.z);
-        cell = make_float3(0.f, 0.f, 0.f);
-      });
-  const float3 add = velocity_increment(d.p, F, xi, vi);
+  const ForceConsts k = force_consts(p);
+  const int3 g = grid_pos(p, xi);
+  const int gx = (int)p.gridSize.x, gy = (int)p.gridSize.y, gz = (int)p.gridSize.z;
+  const int cx = min(max(g.x, 0), gx - 1), cy = min(max(g.y, 0), gy - 1), cz = min(max(g.z, 0), gz - 1);
+  const uint32_t maxpc = p.maxParInCell;
+  const int x0 = max(cx - 1, 0), x1 = min(cx + 1, gx - 1);
+  float3 F = make_float3(0.f, 0.f, 0.f);
+  auto pair = [&](uint32_t j, float3& cell) {
+    const float4 xj = __ldg(pos + j);
+    const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
+    const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
+    if (!(dist2 >= k.h2_out))
+      force_pair_near(k, vi, di, pi, __ldg(vel + j), __ldg(dens + j), __ldg(pres + j), rx, ry, rz,
+                      dist2, cell);
+  };
+  float3 cell = make_float3(0.f, 0.f, 0.f);
+  auto flush = [&]() {
+    F.x = __fadd_rn(F.x, cell.x);
+    F.y = __fadd_rn(F.y, cell.y);
+    F.z = __fadd_rn(F.z, cell.z);
+    cell = make_float3(0.f, 0.f, 0.f);
+  };
+  if (kMask) {
+    // One loop over every set bit of all 9 row masks, in walk order, so a
+    // warp runs max(per-thread neighbour count) iterations rather than the
+    // sum over cells of per-cell maxima.  Cell partial sums are flushed
+    // into F when the cell changes; skipped (zero) partials leave F as is.
+    int r = -1, cur = -1;
+    unsigned long long m = 0;
+    uint32_t s0 = 0, s1 = 0, s2 = 0, b1 = 0, b2 = 0;
+    for (;;) {
+      if (m == 0) {
+        flush();
+        cur = -1;
+        for (++r; r < kRows; ++r) {
+          const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
+          if (z < 0 || z >= gz || y < 0 || y >= gy) continue;
+          m = masks[(size_t)r * N + i];
+          if (m) break;
+        }
+        if (r >= kRows) break;
+        const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
+        const uint32_t row = d.c_off + (uint32_t)(z * (int)p.gridSize_yx + y * gx) + (uint32_t)x0;
+        const int nc = x1 - x0 + 1;
+        const uint32_t n0 = min(__ldg(count + row), maxpc);
+        const uint32_t n1 = nc > 1 ? min(__ldg(count + row + 1), maxpc) : 0u;
+        s0 = __ldg(start + row);
+        s1 = nc > 1 ? __ldg(start + row + 1) : 0u;
+        s2 = nc > 2 ? __ldg(start + row + 2) : 0u;
+        b1 = n0;
+        b2 = n0 + n1;
+      }
+      const uint32_t b = (uint32_t)(__ffsll((long long)m) - 1);
+      m &= m - 1;
+      const int c = b >= b2 ? 2 : (b >= b1 ? 1 : 0);
+      if (c != cur) {
+        flush();
+        cur = c;
+      }
+      const uint32_t j = c == 0 ? s0 + b : (c == 1 ? s1 + (b - b1) : s2 + (b - b2));
+      pair(j, cell);
+    }
+  } else {
+#pragma unroll 1
+    for (int r = 0; r < kRows; ++r) {
+      const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
+      if (z < 0 || z >= gz || y < 0 || y >= gy) continue;
+      const uint32_t row = d.c_off + (uint32_t)(z * (int)p.gridSize_yx + y * gx);
+#pragma unroll 1
+      for (int x = x0; x <= x1; ++x) {
+        const uint32_t c = row + (uint32_t)x;
+        const uint32_t n = min(__ldg(count + c), maxpc);
+        const uint32_t s0 = __ldg(start + c);
+#pragma unroll 4
+        for (uint32_t q = 0; q < n; ++q)
+          if (s0 + q != i) pair(s0 + q, cell);
+        flush();
+      }
+    }
+  }
+  const float3 add = velocity_increment(p, F, xi, vi);
   vel_out[i] = make_float4(__fadd_rn(vi.x, add.x), __fadd_rn(vi.y, add.y), __fadd_rn(vi.z, add.z),
                            __fadd_rn(vi.w, 0.f));
 }
@@ -316,6 +414,7 @@ struct SphSystem {
   uint32_t *key = nullptr, *rank = nullptr, *slot = nullptr;
   uint32_t *count = nullptr, *start = nullptr, *scan_tmp = nullptr;
   float *dens = nullptr, *pres = nullptr;
+  unsigned long long* masks = nullptr;  // kRows x N neighbour masks (null: walks without)
   uint32_t* flags = nullptr;
   double* stats = nullptr;
   float4* staging = nullptr;
@@ -325,7 +424,9 @@ struct SphSystem {
   cudaStream_t stream = nullptr;
   bool own_stream = false;  // created here (destroyed here) or borrowed
   cudaStream_t cap_stream = nullptr;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // two steps, keyed by cp at launch
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // graph_steps steps, keyed by cp at launch
+  uint32_t graph_steps = 2;                         // steps per captured graph (even)
+  int walk_shape = kDefaultShape;                   // index into kWalkBlocks
 };
 
 namespace {
@@ -353,6 +454,27 @@ void drop_graphs(SphSystem* s) {
     }
 }
 
+template <bool kMask, int kThreads, int kMinBlocks, class Mark>
+void launch_walks_shape(SphSystem* s, cudaStream_t st, int b, int v, Mark& mark) {
+  const unsigned g = grid_for(s->N, kThreads);
+  k_density<kMask, kThreads, kMinBlocks><<<g, kThreads, 0, st>>>(
+      s->d_scenes, s->d_poff, s->S, s->N, s->pos[b], s->start, s->count, s->dens, s->pres,
+      s->masks, s->flags);
+  mark();
+  k_force<kMask, kThreads, kMinBlocks><<<g, kThreads, 0, st>>>(
+      s->d_scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->pres, s->start,
+      s->count, s->masks, s->vel[v]);
+}
+
+template <bool kMask, class Mark>
+void launch_walks(SphSystem* s, cudaStream_t st, int b, int v, Mark& mark) {
+  switch (s->walk_shape) {
+    case 0: launch_walks_shape<kMask, 64, 8>(s, st, b, v, mark); break;
+    case 2: launch_walks_shape<kMask, 256, 2>(s, st, b, v, mark); break;
+    default: launch_walks_shape<kMask, 128, 4>(s, st, b, v, mark); break;
+  }
+}
+
 // Enqueues one step on `st`, advancing s->cp.  With `ev` (kStepStages + 1
 // events) an event is recorded before the first stage and after each one.
 constexpr int kStepStages = 6;
@@ -376,11 +498,10 @@ int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
                                  s->key, s->start, s->count, s->slot, s->pos[b], s->vel[1 - v],
                                  s->id[b]);
   mark();
-  k_density<<<gN, kBlock, 0, st>>>(s->d_scenes, s->d_poff, s->S, s->N, s->pos[b], s->start,
-                                   s->count, s->dens, s->pres, s->flags);
-  mark();
-  k_force<<<gN, kBlock, 0, st>>>(s->d_scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v],
-                                 s->dens, s->pres, s->start, s->count, s->vel[v]);
+  if (s->masks)
+    launch_walks<true>(s, st, b, v, mark);
+  else
+    launch_walks<false>(s, st, b, v, mark);
   mark();
   SPH_CUDA(cudaGetLastError(), "step kernels");
   s->cp = b;
@@ -393,8 +514,8 @@ int build_graph(SphSystem* s) {
   if (!s->cap_stream)
     SPH_CUDA(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking), "capture stream");
   SPH_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-  int rc = enqueue_step(s, s->cap_stream);
-  if (rc == SPH_OK) rc = enqueue_step(s, s->cap_stream);
+  int rc = SPH_OK;
+  for (uint32_t k = 0; k < s->graph_steps && rc == SPH_OK; ++k) rc = enqueue_step(s, s->cap_stream);
   cudaGraph_t g = nullptr;
   const cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
   s->cp = cp0;
@@ -412,7 +533,7 @@ void free_all(SphSystem* s) {
   drop_graphs(s);
   void* bufs[] = {s->d_scenes, s->d_poff, s->d_coff, s->pos[0], s->pos[1], s->vel[0], s->vel[1],
                   s->id[0], s->id[1], s->key, s->rank, s->slot, s->count, s->start, s->scan_tmp,
-                  s->dens, s->pres, s->flags, s->stats, s->staging};
+                  s->dens, s->pres, s->masks, s->flags, s->stats, s->staging};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
@@ -468,6 +589,9 @@ int create(const SimParams* scenes, uint32_t count, SphSystem** out) {
   ALLOC(s->dens, n, "density");
   ALLOC(s->pres, n, "pressure");
   ALLOC(s->flags, 1, "flags");
+  bool use_masks = SPH_WALK_MASKS != 0;
+  for (uint32_t i = 0; i < count; ++i) use_masks &= scenes[i].maxParInCell <= kMaskMaxPerCell;
+  if (use_masks) ALLOC(s->masks, (size_t)kRows * n, "neighbour masks");
   ALLOC(s->stats, 4 * (size_t)count, "stats");
 #undef ALLOC
   if (rc == SPH_OK) rc = cuda_check(cudaStreamCreate(&s->stream), "stream");
@@ -603,14 +727,97 @@ int sph_get_array(SphSystem* s, uint32_t which, sph_float4* out, int dst_on_devi
 int sph_step(SphSystem* s, uint32_t steps) {
   if (!s) return fail(SPH_ERR_ARG, "null handle");
   uint32_t done = 0;
-  if (steps >= 2) {
+  const uint32_t gs = s->graph_steps;
+  if (steps >= gs) {
     if (!s->graph[s->cp]) SPH_TRY(build_graph(s));
-    for (; done + 2 <= steps; done += 2)
+    for (; done + gs <= steps; done += gs)
       SPH_CUDA(cudaGraphLaunch(s->graph[s->cp], s->stream), "step graph launch");
   }
   for (; done < steps; ++done) SPH_TRY(enqueue_step(s, s->stream));
   if (steps) s->stepped = true;
   return SPH_OK;
+}
+
+int sph_set_graph_steps(SphSystem* s, uint32_t steps_per_graph) {
+  if (!s || steps_per_graph < 2 || steps_per_graph % 2)
+    return fail(SPH_ERR_ARG, "set_graph_steps: need an even count >= 2");
+  SPH_CUDA(cudaStreamSynchronize(s->stream), "set_graph_steps: drain");
+  drop_graphs(s);
+  s->graph_steps = steps_per_graph;
+  return SPH_OK;
+}
+
+int sph_set_walk_shape(SphSystem* s, uint32_t shape) {
+  if (!s || shape >= (uint32_t)kWalkShapes) return fail(SPH_ERR_ARG, "set_walk_shape: bad shape");
+  SPH_CUDA(cudaStreamSynchronize(s->stream), "set_walk_shape: drain");
+  drop_graphs(s);
+  s->walk_shape = (int)shape;
+  return SPH_OK;
+}
+
+int sph_get_walk_shape(SphSystem* s, uint32_t* shape, uint32_t* threads) {
+  if (!s) return fail(SPH_ERR_ARG, "null handle");
+  if (shape) *shape = (uint32_t)s->walk_shape;
+  if (threads) *threads = (uint32_t)kWalkBlocks[s->walk_shape];
+  return SPH_OK;
+}
+
+int sph_autotune(SphSystem* s, uint32_t trial_steps, float* ms_per_step, uint32_t* chosen) {
+  if (!s || trial_steps == 0) return fail(SPH_ERR_ARG, "autotune: bad arguments");
+  SPH_CUDA(cudaStreamSynchronize(s->stream), "autotune: drain");
+  // Save the state so that tuning leaves the simulation where it was.
+  float4 *sp = nullptr, *sv = nullptr;
+  uint32_t* si = nullptr;
+  int rc = dalloc(&sp, s->N, "autotune: saved positions");
+  if (rc == SPH_OK) rc = dalloc(&sv, s->N, "autotune: saved velocities");
+  if (rc == SPH_OK) rc = dalloc(&si, s->N, "autotune: saved ids");
+  const int cp0 = s->cp, cv0 = s->cv, shape0 = s->walk_shape;
+  const bool stepped0 = s->stepped;
+  if (rc == SPH_OK) {
+    cudaMemcpyAsync(sp, s->pos[cp0], sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream);
+    cudaMemcpyAsync(sv, s->vel[cv0], sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream);
+    cudaMemcpyAsync(si, s->id[cp0], sizeof(uint32_t) * s->N, cudaMemcpyDeviceToDevice, s->stream);
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (rc == SPH_OK) rc = cuda_check(cudaEventCreate(&e0), "autotune: event");
+  if (rc == SPH_OK) rc = cuda_check(cudaEventCreate(&e1), "autotune: event");
+  float best = 0.f;
+  int best_shape = shape0;
+  for (int k = 0; k < kWalkShapes && rc == SPH_OK; ++k) {
+    s->walk_shape = k;
+    rc = enqueue_step(s, s->stream);  // warm-up
+    if (rc == SPH_OK) rc = cuda_check(cudaEventRecord(e0, s->stream), "autotune: record");
+    for (uint32_t t = 0; t < trial_steps && rc == SPH_OK; ++t) rc = enqueue_step(s, s->stream);
+    if (rc == SPH_OK) rc = cuda_check(cudaEventRecord(e1, s->stream), "autotune: record");
+    if (rc == SPH_OK) rc = cuda_check(cudaEventSynchronize(e1), "autotune: sync");
+    float ms = 0.f;
+    if (rc == SPH_OK) rc = cuda_check(cudaEventElapsedTime(&ms, e0, e1), "autotune: elapsed");
+    ms /= (float)trial_steps;
+    if (ms_per_step) ms_per_step[k] = ms;
+    if (rc == SPH_OK && (k == 0 || ms < best)) {
+      best = ms;
+      best_shape = k;
+    }
+    // restore the saved state for the next candidate
+    if (rc == SPH_OK) {
+      s->cp = cp0;
+      s->cv = cv0;
+      cudaMemcpyAsync(s->pos[cp0], sp, sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream);
+      cudaMemcpyAsync(s->vel[cv0], sv, sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream);
+      cudaMemcpyAsync(s->id[cp0], si, sizeof(uint32_t) * s->N, cudaMemcpyDeviceToDevice, s->stream);
+    }
+  }
+  if (rc == SPH_OK) rc = cuda_check(cudaStreamSynchronize(s->stream), "autotune: restore");
+  s->walk_shape = rc == SPH_OK ? best_shape : shape0;
+  s->stepped = stepped0 || rc == SPH_OK;
+  drop_graphs(s);
+  if (chosen) *chosen = (uint32_t)s->walk_shape;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (sp) cudaFree(sp);
+  if (sv) cudaFree(sv);
+  if (si) cudaFree(si);
+  return rc;
 }
 
 int sph_step_timed(SphSystem* s, float* stage_ms, uint32_t nstages) {

@@ -167,6 +167,27 @@ class SPH:
         """cSPH::Update (SPH_Update.cpp:12-81), `steps` times."""
         check(lib().sph_step(self._h, steps))
 
+    def set_graph_steps(self, steps: int) -> None:
+        check(lib().sph_set_graph_steps(self._h, steps))
+
+    WALK_THREADS = (64, 128, 256)
+
+    def set_walk_shape(self, shape: int) -> None:
+        check(lib().sph_set_walk_shape(self._h, shape))
+
+    def walk_shape(self) -> int:
+        sh = ctypes.c_uint32()
+        check(lib().sph_get_walk_shape(self._h, ctypes.byref(sh), None))
+        return sh.value
+
+    def autotune(self, trial_steps: int = 10):
+        """Pick the fastest walk launch shape on this handle's scenes; returns
+        (chosen shape, ms per step of each shape).  State is unchanged."""
+        ms = (ctypes.c_float * 3)()
+        ch = ctypes.c_uint32()
+        check(lib().sph_autotune(self._h, trial_steps, ms, ctypes.byref(ch)))
+        return ch.value, list(ms)
+
     STAGES = ("integrate_count", "scan", "scatter_ids", "place", "density", "force")
 
     def step_timed(self) -> dict:

@@ -178,3 +178,37 @@ def test_million_particle_properties(cuda):
     kv = np.stack([sh[:, 0], ids.astype(np.uint32)], axis=1)
     d64, _ = oracle.density(p, spos, kv, cs, fp64=True)
     np.testing.assert_allclose(dens, d64, rtol=DENS_RTOL, atol=1e-2)
+
+
+def test_walk_shapes_and_graph_lengths_agree(cuda):
+    """Every walk launch shape and every graph length gives the same bits."""
+    w = configs.dambreak_small(side=12)
+    p = Scene.parse(w.xml).params
+    ref = None
+    for shape in (0, 1, 2):
+        for gsteps in (2, 6):
+            with system_from(p, w.pos, w.vel) as s:
+                s.set_walk_shape(shape)
+                s.set_graph_steps(gsteps)
+                s.update(13)  # graph launches plus a direct remainder
+                out = (s.get_array(ARRAY_POS), s.get_array(ARRAY_VEL))
+            if ref is None:
+                ref = out
+            else:
+                np.testing.assert_array_equal(out[0], ref[0])
+                np.testing.assert_array_equal(out[1], ref[1])
+
+
+def test_autotune_keeps_state(cuda):
+    w = configs.dambreak_small(side=12)
+    p = Scene.parse(w.xml).params
+    with system_from(p, w.pos, w.vel) as a, system_from(p, w.pos, w.vel) as b:
+        a.update(5)
+        b.update(5)
+        chosen, ms = a.autotune(trial_steps=4)
+        assert chosen in (0, 1, 2) and all(m > 0 for m in ms)
+        assert a.walk_shape() == chosen
+        a.update(7)
+        b.update(7)
+        np.testing.assert_array_equal(a.get_array(ARRAY_POS), b.get_array(ARRAY_POS))
+        np.testing.assert_array_equal(a.get_array(ARRAY_VEL), b.get_array(ARRAY_VEL))
