@@ -24,6 +24,8 @@ from __future__ import annotations
 import argparse
 import json
 import math
+
+import numpy as np
 import os
 import statistics
 import subprocess
@@ -257,6 +259,71 @@ def run_ensemble(args):
     return 0
 
 
+def measure_learned(sysm, p, stream, args, coarse_steps: int = 50, substeps: int = 4,
+                    tol: float = 0.01):
+    """The learned 4x dt step on the same 1M-particle state: simulated-time
+    throughput (particle-steps of dt per second) against the plain fine-dt
+    step from the same state, and the mean-density error relative to that
+    fine run, sampled every coarse step."""
+    import torch
+    from pibiti_gb300 import learned
+    from pibiti_gb300.sph import ARRAY_POS, ARRAY_VEL, SPH
+    if not os.path.exists(learned.MODEL_PATH):
+        return {"unavailable": "no trained model at pibiti_gb300/models/corrector.npz"}
+    model = learned.Model.load()
+    n = sysm.n
+    tp = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    tv = torch.empty_like(tp)
+    sysm.get_array(ARRAY_POS, tp)
+    sysm.get_array(ARRAY_VEL, tv)
+    torch.cuda.synchronize()
+    res = {}
+    rho = {}
+    for mode in ("fine", "learned"):
+        h = SPH(p, stream=stream)
+        h.set_array(ARRAY_POS, tp)
+        h.set_array(ARRAY_VEL, tv)
+        h.update(2)  # first steps of a fresh handle (graph build), excluded
+        if mode == "learned":
+            model.install(h)
+            learned.learned_step(h, 1, substeps, tol)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fb = 0
+        if mode == "fine":
+            h.update(substeps * coarse_steps)
+        else:
+            fb = learned.learned_step(h, coarse_steps, substeps, tol)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        res[mode] = {"value": n * substeps * coarse_steps / (ms / 1e3), "ms": ms, "fallbacks": fb}
+        h.close()
+        # density trajectories for the error (untimed, sampled every coarse step)
+        h = SPH(p, stream=stream)
+        h.set_array(ARRAY_POS, tp)
+        h.set_array(ARRAY_VEL, tv)
+        traj = []
+        if mode == "learned":
+            model.install(h)
+        for _ in range(coarse_steps):
+            if mode == "fine":
+                h.update(substeps)
+            else:
+                learned.learned_step(h, 1, substeps, tol)
+            traj.append(h.stats()[0][1])
+        rho[mode] = np.asarray(traj)
+        h.close()
+    err = float(np.max(np.abs(rho["learned"] - rho["fine"]) / rho["fine"]))
+    return {"unit": UNIT, "value": res["learned"]["value"], "fine_value": res["fine"]["value"],
+            "speedup_vs_fine": res["learned"]["value"] / res["fine"]["value"],
+            "mean_density_err": err, "fallbacks": res["learned"]["fallbacks"],
+            "coarse_steps": coarse_steps, "substeps": substeps, "tol": tol,
+            "note": "simulated-time throughput: particle-steps of dt per second; error = max over "
+                    "coarse steps of |mean density - fine-dt mean density| / fine"}
+
+
 def workload_config(p, n=None):
     cfg = {"workload": "double dam break, 1,048,576 particles: two 64x128x64 lattices at "
                        "spacing 0.5h (h=0.0457 m) in a 6.0x3.4x1.7 m box, +-1% jitter, "
@@ -404,6 +471,8 @@ def main():
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     e2e_value = world * n * args.e2e_steps / (float(t.item()) / 1e3)
 
+    learned = measure_learned(sysm, p, stream, args) if rank == 0 else None
+
     st = sysm.stats()[0]
     flags = sysm.flags()
     if rank == 0:
@@ -420,6 +489,7 @@ def main():
             "gpu_launches": KERNELS_PER_STEP * args.steps,
             "warm_ms_per_step": warm_ms,
             "wall_s_timed_loop": wall,
+            "learned": learned,
             "state_check": {"kinetic_energy": st[0], "mean_density": st[1],
                             "max_density_dev": st[2], "nonfinite": st[3], "flags": flags},
         }

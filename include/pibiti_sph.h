@@ -205,6 +205,53 @@ int sph_stats(SphSystem* sys, double* out);
 int sph_flags(SphSystem* sys, uint32_t* flags);
 
 /* ======================================================================
+ * 4. Learned corrector: a per-particle MLP 16 -> 64 -> 64 -> 3 (tanh) on the
+ *    tensor cores, BF16 operands and FP32 accumulation.  No counterpart in
+ *    the reference: it lets a step of 4x dt be corrected towards four steps
+ *    of dt.  All pointers are device pointers.
+ * ==================================================================== */
+#define SPH_MLP_IN 16
+#define SPH_MLP_HIDDEN 64
+#define SPH_MLP_OUT 3
+
+/* Number of FP32 parameters: W1[16][64] b1[64] W2[64][64] b2[64] W3[64][3]
+   b3[3], in that order (5443). */
+int sph_mlp_param_count(void);
+/* Bytes of the packed BF16 image the kernels read. */
+int sph_mlp_packed_bytes(void);
+/* FP32 parameters -> packed BF16 image. */
+int sph_mlp_pack(const float* params, void* packed, void* stream);
+/* y[n][3] = MLP(x[n][16]); x is BF16 (uint16 bit patterns), y FP32. */
+int sph_mlp_forward(const void* packed, const uint16_t* x, uint32_t n, float* y, void* stream);
+/* One pass over n samples of the loss mean((y - target)^2) (over all 3n
+   outputs): adds d loss / d params to grad[5443] and the loss to *loss
+   (both FP32, zeroed by the caller). */
+int sph_mlp_train_pass(const void* packed, const uint16_t* x, const float* target, uint32_t n,
+                       float* grad, float* loss, void* stream);
+/* Adam step `step` (1-based) on the FP32 parameters with moments m, v. */
+int sph_mlp_adam(float* params, float* m, float* v, const float* grad, float lr, float beta1,
+                 float beta2, float eps, uint32_t step, void* stream);
+
+/* The learned step on a system handle.  A coarse step is one whole step
+   with the time step multiplied by `substeps` whose force pass also writes
+   16 features per particle; the MLP then adds a velocity correction
+   y * out_scale * |g| * dt_coarse.  After every coarse step a density check
+   runs: if any scene's mean density moved by more than `tol` (relative)
+   over the step, or any value is not finite, the state is restored and the
+   scene set advances by `substeps` plain steps of the original time step
+   instead (counted in *fallbacks). */
+/* Model: FP32 parameters (host, sph_mlp_param_count() floats), feature
+   mean[16] and 1/std[16] (host, 32 floats), out_scale[3]. */
+int sph_learned_set_model(SphSystem* sys, const float* params, const float* feat_stats,
+                          const float* out_scale);
+int sph_learned_step(SphSystem* sys, uint32_t coarse_steps, uint32_t substeps, float tol,
+                     uint32_t* fallbacks);
+/* Training data: one coarse step (no correction) that writes the raw FP32
+   features (device, N x 16, sorted order) and the original index of each
+   sorted slot (device, N); the state advances by that coarse step. */
+int sph_features_step(SphSystem* sys, uint32_t substeps, float* feat_raw, uint32_t* ids);
+
+/* ======================================================================
  * 3. Scenes (Scene / cSPH::LoadScenes replacement, host only)
  * ==================================================================== */
 

@@ -84,6 +84,16 @@ SIGNATURES = {
     "sph_scene_default": [P(SimParams), P(SceneInfo)],
     "sph_scene_default_index": [ctypes.c_char_p, P(i32)],
     "sph_scene_reset": [P(SimParams), P(SceneInfo), i32, ctypes.c_uint64, vp, vp, P(u32)],
+    "sph_mlp_param_count": [],
+    "sph_mlp_packed_bytes": [],
+    "sph_mlp_pack": [vp, vp, vp],
+    "sph_mlp_forward": [vp, vp, u32, vp, vp],
+    "sph_mlp_train_pass": [vp, vp, vp, u32, vp, vp, vp],
+    "sph_mlp_adam": [vp, vp, vp, vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                     ctypes.c_float, u32, vp],
+    "sph_learned_set_model": [vp, vp, vp, vp],
+    "sph_learned_step": [vp, u32, u32, ctypes.c_float, P(u32)],
+    "sph_features_step": [vp, u32, vp, vp],
     "sph_last_error": [],
     "sph_version": [],
 }

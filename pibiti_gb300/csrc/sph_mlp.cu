@@ -1,0 +1,479 @@
+// sph_mlp.cu -- the per-particle MLP corrector (16 -> 64 -> 64 -> 3, tanh)
+// on the tensor cores: BF16 operands, FP32 accumulation, mma.sync
+// m16n8k16 (one warp = 16 particles per tile).
+//
+// Parameters are kept in FP32 (training master copy) in one vector:
+//   W1[16][64] b1[64] W2[64][64] b2[64] W3[64][3] b3[3]   (5443 floats)
+// and packed to a BF16 image for the kernels (sph_mlp_pack):
+//   WT1[64][24]  W1 transposed (out-major), forward operand of layer 1
+//   WT2[64][72]  W2 transposed, forward operand of layer 2
+//   W2r[64][72]  W2 in-major, backward operand (dH1 = dZ2 W2^T)
+//   WT3[8][72]   W3 transposed, 3 outputs padded to 8, forward operand
+//   W3r[64][24]  W3 in-major, outputs padded, backward operand
+//   b1[64] b2[64] b3[8]   FP32
+// Row strides are padded (24, 72 halves) so the fragment loads of a warp
+// fall in distinct shared-memory banks.
+//
+// Fragment layout of mma.m16n8k16 (g = lane / 4, t = lane % 4):
+//   A 16x16: a0 (g, 2t..2t+1) a1 (g+8, 2t..) a2 (g, 2t+8..) a3 (g+8, 2t+8..)
+//   B 16x8 : b0 (k 2t..2t+1, n g) b1 (k 2t+8.., n g)
+//   C 16x8 : c0 (g, 2t) c1 (g, 2t+1) c2 (g+8, 2t) c3 (g+8, 2t+1)
+// The C fragments of two adjacent n-tiles are exactly the A fragment of the
+// next layer's k-tile, so activations stay in registers between layers.
+#include <cstdint>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "sph_internal.h"
+
+namespace sph {
+namespace mlp {
+
+constexpr int IN = 16, HID = 64, OUT = 3, OUTP = 8;
+constexpr int S1 = 24, S2 = 72, S3r = 24;  // padded row strides (halves)
+// packed image offsets (halves)
+constexpr int oWT1 = 0;
+constexpr int oWT2 = oWT1 + HID * S1;
+constexpr int oW2r = oWT2 + HID * S2;
+constexpr int oWT3 = oW2r + HID * S2;
+constexpr int oW3r = oWT3 + OUTP * S2;
+constexpr int kHalves = oW3r + HID * S3r;                 // 12864
+constexpr int kBiasFloats = HID + HID + OUTP;             // 136
+constexpr int kPackedBytes = kHalves * 2 + kBiasFloats * 4;
+// canonical FP32 parameter offsets
+constexpr int pW1 = 0, pB1 = pW1 + IN * HID, pW2 = pB1 + HID, pB2 = pW2 + HID * HID,
+              pW3 = pB2 + HID, pB3 = pW3 + HID * OUT, kParams = pB3 + OUT;  // 5443
+
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+__device__ __forceinline__ float lo_of(uint32_t u) { return __uint_as_float(u << 16); }
+__device__ __forceinline__ float hi_of(uint32_t u) { return __uint_as_float(u & 0xffff0000u); }
+__device__ __forceinline__ float bf(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
+
+__device__ __forceinline__ void mma(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t ld32(const uint16_t* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+// Packs the FP32 parameters into the BF16 kernel image.
+__global__ void k_pack(const float* __restrict__ prm, uint16_t* __restrict__ img) {
+  uint16_t* w = img;
+  float* bias = reinterpret_cast<float*>(img + kHalves);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < kHalves + kBiasFloats;
+       e += gridDim.x * blockDim.x) {
+    if (e >= kHalves) {
+      const int b = e - kHalves;
+      float v = 0.f;
+      if (b < HID) v = prm[pB1 + b];
+      else if (b < 2 * HID) v = prm[pB2 + b - HID];
+      else if (b - 2 * HID < OUT) v = prm[pB3 + b - 2 * HID];
+      bias[b] = v;
+      continue;
+    }
+    float v = 0.f;
+    if (e < oWT2) {  // WT1[o][i] = W1[i][o]
+      const int o = (e - oWT1) / S1, i = (e - oWT1) % S1;
+      if (i < IN) v = prm[pW1 + i * HID + o];
+    } else if (e < oW2r) {  // WT2[o][i] = W2[i][o]
+      const int o = (e - oWT2) / S2, i = (e - oWT2) % S2;
+      if (i < HID) v = prm[pW2 + i * HID + o];
+    } else if (e < oWT3) {  // W2r[i][o] = W2[i][o]
+      const int i = (e - oW2r) / S2, o = (e - oW2r) % S2;
+      if (o < HID) v = prm[pW2 + i * HID + o];
+    } else if (e < oW3r) {  // WT3[o][i] = W3[i][o]
+      const int o = (e - oWT3) / S2, i = (e - oWT3) % S2;
+      if (o < OUT && i < HID) v = prm[pW3 + i * OUT + o];
+    } else {  // W3r[i][o] = W3[i][o]
+      const int i = (e - oW3r) / S3r, o = (e - oW3r) % S3r;
+      if (o < OUT) v = prm[pW3 + i * OUT + o];
+    }
+    w[e] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+  }
+}
+
+__device__ __forceinline__ void load_image(const uint16_t* __restrict__ img, uint16_t* sw) {
+  const uint4* src = reinterpret_cast<const uint4*>(img);
+  uint4* dst = reinterpret_cast<uint4*>(sw);
+  for (int k = threadIdx.x; k < kPackedBytes / 16; k += blockDim.x) dst[k] = src[k];
+  __syncthreads();
+}
+
+// Forward pass of one 16-row tile; x is BF16 [rows][16].  Returns the
+// output C fragment and leaves the hidden activations (BF16 A fragments).
+struct Fwd {
+  uint32_t h1[4][4];  // A fragments of layer 2 (k-tiles 0..3)
+  uint32_t h2[4][4];  // A fragments of layer 3
+  float y[4];         // C fragment of the output (cols 2t, 2t+1; rows g, g+8)
+};
+
+__device__ __forceinline__ void forward_tile(const uint16_t* sw, const float* sb,
+                                             const uint16_t* __restrict__ x, uint32_t row0,
+                                             uint32_t n, Fwd& f) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const uint32_t r0 = row0 + g, r1 = row0 + g + 8;
+  uint32_t a[4];
+  a[0] = r0 < n ? ld32(x + (size_t)r0 * IN + 2 * t) : 0u;
+  a[1] = r1 < n ? ld32(x + (size_t)r1 * IN + 2 * t) : 0u;
+  a[2] = r0 < n ? ld32(x + (size_t)r0 * IN + 2 * t + 8) : 0u;
+  a[3] = r1 < n ? ld32(x + (size_t)r1 * IN + 2 * t + 8) : 0u;
+  // layer 1: [16 x 16] x [16 x 64]
+#pragma unroll
+  for (int nt = 0; nt < 8; ++nt) {
+    const float b0 = sb[8 * nt + 2 * t], b1 = sb[8 * nt + 2 * t + 1];
+    float c[4] = {b0, b1, b0, b1};
+    const uint16_t* w = sw + oWT1 + (8 * nt + g) * S1 + 2 * t;
+    mma(c, a, ld32(w), ld32(w + 8));
+    const int kt = nt >> 1;
+    if ((nt & 1) == 0) {
+      f.h1[kt][0] = pack2(tanhf(c[0]), tanhf(c[1]));
+      f.h1[kt][1] = pack2(tanhf(c[2]), tanhf(c[3]));
+    } else {
+      f.h1[kt][2] = pack2(tanhf(c[0]), tanhf(c[1]));
+      f.h1[kt][3] = pack2(tanhf(c[2]), tanhf(c[3]));
+    }
+  }
+  // layer 2: [16 x 64] x [64 x 64]
+#pragma unroll
+  for (int nt = 0; nt < 8; ++nt) {
+    const float b0 = sb[HID + 8 * nt + 2 * t], b1 = sb[HID + 8 * nt + 2 * t + 1];
+    float c[4] = {b0, b1, b0, b1};
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+      const uint16_t* w = sw + oWT2 + (8 * nt + g) * S2 + 16 * kt + 2 * t;
+      mma(c, f.h1[kt], ld32(w), ld32(w + 8));
+    }
+    const int kt = nt >> 1;
+    if ((nt & 1) == 0) {
+      f.h2[kt][0] = pack2(tanhf(c[0]), tanhf(c[1]));
+      f.h2[kt][1] = pack2(tanhf(c[2]), tanhf(c[3]));
+    } else {
+      f.h2[kt][2] = pack2(tanhf(c[0]), tanhf(c[1]));
+      f.h2[kt][3] = pack2(tanhf(c[2]), tanhf(c[3]));
+    }
+  }
+  // layer 3: [16 x 64] x [64 x 8]
+  {
+    const float b0 = sb[2 * HID + 2 * t], b1 = sb[2 * HID + 2 * t + 1];
+    f.y[0] = b0;
+    f.y[1] = b1;
+    f.y[2] = b0;
+    f.y[3] = b1;
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+      const uint16_t* w = sw + oWT3 + g * S2 + 16 * kt + 2 * t;
+      mma(f.y, f.h2[kt], ld32(w), ld32(w + 8));
+    }
+  }
+}
+
+// y[n][3] = MLP(x[n][16]).
+__global__ void __launch_bounds__(128) k_forward(const uint16_t* __restrict__ img,
+                                                 const uint16_t* __restrict__ x, uint32_t n,
+                                                 float* __restrict__ y) {
+  extern __shared__ __align__(16) uint16_t smem[];
+  load_image(img, smem);
+  const float* sb = reinterpret_cast<const float*>(smem + kHalves);
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile * 16 < n;
+       tile += warps) {
+    Fwd f;
+    forward_tile(smem, sb, x, tile * 16, n, f);
+    const uint32_t r0 = tile * 16 + g, r1 = r0 + 8;
+    const int c0 = 2 * t;
+    if (c0 < OUT) {
+      if (r0 < n) y[(size_t)r0 * OUT + c0] = f.y[0];
+      if (r1 < n) y[(size_t)r1 * OUT + c0] = f.y[2];
+    }
+    if (c0 + 1 < OUT) {
+      if (r0 < n) y[(size_t)r0 * OUT + c0 + 1] = f.y[1];
+      if (r1 < n) y[(size_t)r1 * OUT + c0 + 1] = f.y[3];
+    }
+  }
+}
+
+// One training pass over n samples: loss = sum((y - target)^2) * inv_count,
+// gradients of that loss added (FP32 atomics) into grad[kParams], loss into
+// *loss.  Per block: 4 warps x 16 samples per tile; forward and backward in
+// registers, activations and their gradients staged in shared memory
+// (BF16) for the weight-gradient products, which each warp accumulates for
+// its quarter of every weight matrix over all tiles of the block.
+constexpr int kTrainThreads = 128, kTileRows = 64;
+constexpr int SA = 72;  // staging row stride (halves) for 64-wide rows
+constexpr int SX = 24;  // staging row stride for 16-wide / 8-wide rows
+constexpr int kStageHalves = kTileRows * (SX + SA + SA + SA + SA + SX);
+
+__global__ void __launch_bounds__(kTrainThreads) k_train(const uint16_t* __restrict__ img,
+                                                         const uint16_t* __restrict__ x,
+                                                         const float* __restrict__ target,
+                                                         uint32_t n, float inv_count,
+                                                         float* __restrict__ grad,
+                                                         float* __restrict__ loss) {
+  extern __shared__ __align__(16) uint16_t smem[];
+  load_image(img, smem);
+  const float* sb = reinterpret_cast<const float*>(smem + kHalves);
+  uint16_t* sX = smem + kHalves + 2 * kBiasFloats;
+  uint16_t* sH1 = sX + kTileRows * SX;
+  uint16_t* sH2 = sH1 + kTileRows * SA;
+  uint16_t* sZ1 = sH2 + kTileRows * SA;
+  uint16_t* sZ2 = sZ1 + kTileRows * SA;
+  uint16_t* sY = sZ2 + kTileRows * SA;
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, w = threadIdx.x >> 5;
+  float aW2[8][4] = {}, aW1[2][4] = {}, aW3[4] = {};
+  float bsum = 0.f, lsum = 0.f;  // bias gradient of column threadIdx.x (see below), loss
+  const uint32_t tiles = (n + kTileRows - 1) / kTileRows;
+  for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const uint32_t row0 = tile * kTileRows + 16 * w;
+    Fwd f;
+    forward_tile(smem, sb, x, row0, n, f);
+    const uint32_t r0 = row0 + g, r1 = row0 + g + 8;
+    // dL/dy for the 3 valid columns
+    float dy[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t r = q < 2 ? r0 : r1;
+      const int c = 2 * t + (q & 1);
+      float d = 0.f;
+      if (r < n && c < OUT) {
+        const float e = f.y[q] - target[(size_t)r * OUT + c];
+        lsum = fmaf(e, e, lsum);
+        d = 2.f * e * inv_count;
+      }
+      dy[q] = d;
+    }
+    uint32_t ady[4] = {pack2(dy[0], dy[1]), pack2(dy[2], dy[3]), 0u, 0u};
+    // dH2 = dY W3^T, dZ2 = dH2 (1 - h2^2)
+    uint32_t az2[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+      const uint16_t* wp = smem + oW3r + (8 * nt + g) * S3r + 2 * t;
+      mma(c, ady, ld32(wp), ld32(wp + 8));
+      const int kt = nt >> 1, hi = nt & 1;
+      const uint32_t h01 = f.h2[kt][hi ? 2 : 0], h23 = f.h2[kt][hi ? 3 : 1];
+      const float z0 = c[0] * (1.f - lo_of(h01) * lo_of(h01));
+      const float z1 = c[1] * (1.f - hi_of(h01) * hi_of(h01));
+      const float z2 = c[2] * (1.f - lo_of(h23) * lo_of(h23));
+      const float z3 = c[3] * (1.f - hi_of(h23) * hi_of(h23));
+      az2[kt][hi ? 2 : 0] = pack2(z0, z1);
+      az2[kt][hi ? 3 : 1] = pack2(z2, z3);
+    }
+    // dH1 = dZ2 W2^T, dZ1 = dH1 (1 - h1^2)
+    uint32_t az1[4][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) {
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int kt = 0; kt < 4; ++kt) {
+        const uint16_t* wp = smem + oW2r + (8 * nt + g) * S2 + 16 * kt + 2 * t;
+        mma(c, az2[kt], ld32(wp), ld32(wp + 8));
+      }
+      const int kt = nt >> 1, hi = nt & 1;
+      const uint32_t h01 = f.h1[kt][hi ? 2 : 0], h23 = f.h1[kt][hi ? 3 : 1];
+      const float z0 = c[0] * (1.f - lo_of(h01) * lo_of(h01));
+      const float z1 = c[1] * (1.f - hi_of(h01) * hi_of(h01));
+      const float z2 = c[2] * (1.f - lo_of(h23) * lo_of(h23));
+      const float z3 = c[3] * (1.f - hi_of(h23) * hi_of(h23));
+      az1[kt][hi ? 2 : 0] = pack2(z0, z1);
+      az1[kt][hi ? 3 : 1] = pack2(z2, z3);
+    }
+    // stage this warp's 16 rows: X, H1, H2, dZ1, dZ2, dY (BF16)
+    {
+      const int lr0 = 16 * w + g, lr1 = lr0 + 8;
+      auto st = [&](uint16_t* base, int stride, int row, int col, uint32_t v) {
+        *reinterpret_cast<uint32_t*>(base + row * stride + col) = v;
+      };
+      st(sX, SX, lr0, 2 * t, r0 < n ? ld32(x + (size_t)r0 * IN + 2 * t) : 0u);
+      st(sX, SX, lr1, 2 * t, r1 < n ? ld32(x + (size_t)r1 * IN + 2 * t) : 0u);
+      st(sX, SX, lr0, 2 * t + 8, r0 < n ? ld32(x + (size_t)r0 * IN + 2 * t + 8) : 0u);
+      st(sX, SX, lr1, 2 * t + 8, r1 < n ? ld32(x + (size_t)r1 * IN + 2 * t + 8) : 0u);
+#pragma unroll
+      for (int kt = 0; kt < 4; ++kt) {
+        const int c0 = 16 * kt + 2 * t, c1 = c0 + 8;
+        st(sH1, SA, lr0, c0, f.h1[kt][0]); st(sH1, SA, lr1, c0, f.h1[kt][1]);
+        st(sH1, SA, lr0, c1, f.h1[kt][2]); st(sH1, SA, lr1, c1, f.h1[kt][3]);
+        st(sH2, SA, lr0, c0, f.h2[kt][0]); st(sH2, SA, lr1, c0, f.h2[kt][1]);
+        st(sH2, SA, lr0, c1, f.h2[kt][2]); st(sH2, SA, lr1, c1, f.h2[kt][3]);
+        st(sZ1, SA, lr0, c0, az1[kt][0]); st(sZ1, SA, lr1, c0, az1[kt][1]);
+        st(sZ1, SA, lr0, c1, az1[kt][2]); st(sZ1, SA, lr1, c1, az1[kt][3]);
+        st(sZ2, SA, lr0, c0, az2[kt][0]); st(sZ2, SA, lr1, c0, az2[kt][1]);
+        st(sZ2, SA, lr0, c1, az2[kt][2]); st(sZ2, SA, lr1, c1, az2[kt][3]);
+      }
+      st(sY, SX, lr0, 2 * t, ady[0]);
+      st(sY, SX, lr1, 2 * t, ady[1]);
+    }
+    __syncthreads();
+    // weight gradients over the block's 64 samples (K = samples)
+    auto afrag = [&](const uint16_t* base, int stride, int m0, int kt, uint32_t a[4]) {
+      // A[m][k] = base[k][m]: rows m0+g, m0+g+8; samples 16kt + 2t (+1, +8, +9)
+      const int s0 = 16 * kt + 2 * t;
+      const uint16_t* p = base + m0 + g;
+      a[0] = (uint32_t)p[s0 * stride] | ((uint32_t)p[(s0 + 1) * stride] << 16);
+      a[1] = (uint32_t)p[s0 * stride + 8] | ((uint32_t)p[(s0 + 1) * stride + 8] << 16);
+      a[2] = (uint32_t)p[(s0 + 8) * stride] | ((uint32_t)p[(s0 + 9) * stride] << 16);
+      a[3] = (uint32_t)p[(s0 + 8) * stride + 8] | ((uint32_t)p[(s0 + 9) * stride + 8] << 16);
+    };
+    auto bfrag = [&](const uint16_t* base, int stride, int n0, int kt, uint32_t& b0, uint32_t& b1) {
+      // B[k][n] = base[k][n]: n = n0 + g; samples 16kt + 2t (+1), +8 (+9)
+      const int s0 = 16 * kt + 2 * t;
+      const uint16_t* p = base + n0 + g;
+      b0 = (uint32_t)p[s0 * stride] | ((uint32_t)p[(s0 + 1) * stride] << 16);
+      b1 = (uint32_t)p[(s0 + 8) * stride] | ((uint32_t)p[(s0 + 9) * stride] << 16);
+    };
+#pragma unroll
+    for (int kt = 0; kt < 4; ++kt) {
+      uint32_t a[4], b0, b1;
+      // dW2[16w.., :] += H1^T dZ2
+      afrag(sH1, SA, 16 * w, kt, a);
+#pragma unroll
+      for (int nt = 0; nt < 8; ++nt) {
+        bfrag(sZ2, SA, 8 * nt, kt, b0, b1);
+        mma(aW2[nt], a, b0, b1);
+      }
+      // dW3[16w.., 0..7] += H2^T dY
+      afrag(sH2, SA, 16 * w, kt, a);
+      bfrag(sY, SX, 0, kt, b0, b1);
+      mma(aW3, a, b0, b1);
+      // dW1[0..15, 16w..16w+15] += X^T dZ1
+      afrag(sX, SX, 0, kt, a);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        bfrag(sZ1, SA, 16 * w + 8 * q, kt, b0, b1);
+        mma(aW1[q], a, b0, b1);
+      }
+    }
+    // bias gradients: thread c < 64 sums column c of dZ1, 64 <= c < 128
+    // column c-64 of dZ2; column sums of dY are added by threads 0..2 below.
+    {
+      const int c = threadIdx.x;
+      const uint16_t* col = c < 64 ? sZ1 + c : sZ2 + (c - 64);
+      float s = 0.f;
+      for (int r = 0; r < kTileRows; ++r) s += bf(col[r * SA]);
+      bsum += s;
+    }
+    if (threadIdx.x < OUT) {
+      float s = 0.f;
+      for (int r = 0; r < kTileRows; ++r) s += bf(sY[r * SX + threadIdx.x]);
+      atomicAdd(grad + pB3 + threadIdx.x, s);
+    }
+    __syncthreads();
+  }
+  // flush the block's partial gradients
+#pragma unroll
+  for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = 16 * w + g + (q >= 2 ? 8 : 0), o = 8 * nt + 2 * t + (q & 1);
+      atomicAdd(grad + pW2 + i * HID + o, aW2[nt][q]);
+    }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = 16 * w + g + (q >= 2 ? 8 : 0), o = 2 * t + (q & 1);
+    if (o < OUT) atomicAdd(grad + pW3 + i * OUT + o, aW3[q]);
+  }
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = g + (q >= 2 ? 8 : 0), o = 16 * w + 8 * h + 2 * t + (q & 1);
+      atomicAdd(grad + pW1 + i * HID + o, aW1[h][q]);
+    }
+  atomicAdd(grad + (threadIdx.x < 64 ? pB1 + threadIdx.x : pB2 + threadIdx.x - 64), bsum);
+  for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+  if (lane == 0) atomicAdd(loss, lsum * inv_count);
+}
+
+// Adam on the FP32 master parameters.
+__global__ void k_adam(float* __restrict__ prm, float* __restrict__ m, float* __restrict__ v,
+                       const float* __restrict__ grad, int count, float lr, float beta1,
+                       float beta2, float eps, float bc1, float bc2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float gr = grad[i];
+  const float mi = beta1 * m[i] + (1.f - beta1) * gr;
+  const float vi = beta2 * v[i] + (1.f - beta2) * gr * gr;
+  m[i] = mi;
+  v[i] = vi;
+  prm[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+}
+
+}  // namespace mlp
+}  // namespace sph
+
+using namespace sph;
+using namespace sph::mlp;
+
+namespace {
+constexpr int kTrainSmem = kPackedBytes + kStageHalves * 2;
+
+int mlp_kernels_ready() {
+  static int rc = -1;
+  if (rc < 0) {
+    rc = cuda_check(cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kTrainSmem),
+                    "mlp: shared memory limit");
+  }
+  return rc;
+}
+
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+}  // namespace
+
+extern "C" {
+
+int sph_mlp_param_count(void) { return kParams; }
+int sph_mlp_packed_bytes(void) { return kPackedBytes; }
+
+int sph_mlp_pack(const float* params, void* packed, void* stream) {
+  if (!params || !packed) return fail(SPH_ERR_ARG, "mlp_pack: null pointer");
+  k_pack<<<26, 512, 0, (cudaStream_t)stream>>>(params, (uint16_t*)packed);
+  return cuda_check(cudaGetLastError(), "mlp_pack");
+}
+
+int sph_mlp_forward(const void* packed, const uint16_t* x, uint32_t n, float* y, void* stream) {
+  if (!packed || (!x && n) || (!y && n)) return fail(SPH_ERR_ARG, "mlp_forward: null pointer");
+  if (n == 0) return SPH_OK;
+  const uint32_t tiles = (n + 15) / 16;
+  const uint32_t blocks = (uint32_t)min((long long)(tiles + 3) / 4, (long long)sm_count() * 8);
+  k_forward<<<blocks, 128, kPackedBytes, (cudaStream_t)stream>>>((const uint16_t*)packed, x, n, y);
+  return cuda_check(cudaGetLastError(), "mlp_forward");
+}
+
+int sph_mlp_train_pass(const void* packed, const uint16_t* x, const float* target, uint32_t n,
+                       float* grad, float* loss, void* stream) {
+  if (!packed || !x || !target || !grad || !loss) return fail(SPH_ERR_ARG, "mlp_train: null pointer");
+  if (n == 0) return SPH_OK;
+  SPH_TRY(mlp_kernels_ready());
+  const uint32_t tiles = (n + kTileRows - 1) / kTileRows;
+  const uint32_t blocks = (uint32_t)min((long long)tiles, (long long)sm_count() * 3);
+  k_train<<<blocks, kTrainThreads, kTrainSmem, (cudaStream_t)stream>>>(
+      (const uint16_t*)packed, x, target, n, 1.0f / (3.0f * (float)n), grad, loss);
+  return cuda_check(cudaGetLastError(), "mlp_train");
+}
+
+int sph_mlp_adam(float* params, float* m, float* v, const float* grad, float lr, float beta1,
+                 float beta2, float eps, uint32_t step, void* stream) {
+  if (!params || !m || !v || !grad || step == 0) return fail(SPH_ERR_ARG, "mlp_adam: bad arguments");
+  const float bc1 = 1.f - powf(beta1, (float)step), bc2 = 1.f - powf(beta2, (float)step);
+  k_adam<<<(kParams + 255) / 256, 256, 0, (cudaStream_t)stream>>>(params, m, v, grad, kParams, lr,
+                                                                  beta1, beta2, eps, bc1, bc2);
+  return cuda_check(cudaGetLastError(), "mlp_adam");
+}
+
+}  // extern "C"

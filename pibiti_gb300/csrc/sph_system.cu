@@ -30,6 +30,8 @@
 #include <cstring>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "sph_device.cuh"
 #include "sph_internal.h"
 
@@ -96,6 +98,90 @@ k_scatter_ids(uint32_t N, const uint32_t* __restrict__ key, const uint32_t* __re
   slot[start[key[i]] + rank[i]] = id[i];
 }
 
+// Cells with more than kLinearRank particles get their id segment of
+// `slot` sorted (k_sort_cells / k_sort_big_cells) so that k_place finds a
+// particle's rank by binary search; smaller cells are counted linearly.
+// Sorting is by original index, the order the reference's stable sort
+// gives within a cell.
+constexpr uint32_t kLinearRank = 32;
+constexpr uint32_t kWarpSortMax = 1024;   // sorted by one warp in shared memory
+constexpr uint32_t kBlockSortMax = 16384; // sorted by one block in shared memory
+constexpr int kSortWarps = 4;
+constexpr int kBigThreads = 1024;
+
+__device__ __forceinline__ uint32_t pow2_at_least(uint32_t n) {
+  return n <= 1 ? 1u : 1u << (32 - __clz(n - 1));
+}
+
+// Bitonic sort of buf[0, m) (m a power of two) by `lanes` cooperating
+// threads with index `me`; `sync` orders the stages.
+template <class Sync>
+__device__ __forceinline__ void bitonic(uint32_t* buf, uint32_t m, uint32_t me, uint32_t lanes,
+                                        Sync sync) {
+  for (uint32_t size = 2; size <= m; size <<= 1)
+    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+      for (uint32_t t = me; t < (m >> 1); t += lanes) {
+        const uint32_t i = 2 * stride * (t / stride) + (t % stride), j = i + stride;
+        const bool up = (i & size) == 0;
+        const uint32_t a = buf[i], b = buf[j];
+        if ((a > b) == up) {
+          buf[i] = b;
+          buf[j] = a;
+        }
+      }
+      sync();
+    }
+}
+
+__global__ void __launch_bounds__(kSortWarps * 32)
+k_sort_cells(uint32_t C, const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
+             uint32_t* __restrict__ slot, uint32_t* __restrict__ big_list,
+             uint32_t* __restrict__ big_count) {
+  __shared__ uint32_t buf[kSortWarps][kWarpSortMax];
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (uint32_t c = blockIdx.x * kSortWarps + w; c < C; c += gridDim.x * kSortWarps) {
+    const uint32_t n = count[c];
+    if (n <= kLinearRank) continue;
+    if (n > kWarpSortMax) {
+      if (lane == 0) big_list[atomicAdd(big_count, 1u)] = c;
+      continue;
+    }
+    const uint32_t s0 = start[c], m = pow2_at_least(n);
+    uint32_t* b = buf[w];
+    for (uint32_t k = lane; k < m; k += 32) b[k] = k < n ? slot[s0 + k] : 0xffffffffu;
+    __syncwarp();
+    bitonic(b, m, lane, 32, [] { __syncwarp(); });
+    for (uint32_t k = lane; k < n; k += 32) slot[s0 + k] = b[k];
+    __syncwarp();
+  }
+}
+
+// Cells beyond one warp's buffer: one block each, in shared memory up to
+// kBlockSortMax ids, beyond that in `scratch` (2 words per particle, so the
+// padded segments of different cells never overlap).
+__global__ void __launch_bounds__(kBigThreads)
+k_sort_big_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
+                 uint32_t* __restrict__ slot, const uint32_t* __restrict__ big_list,
+                 const uint32_t* __restrict__ big_count, uint32_t* __restrict__ scratch) {
+  extern __shared__ uint32_t sbuf[];
+  const uint32_t nbig = *big_count;
+  for (uint32_t q = blockIdx.x; q < nbig; q += gridDim.x) {
+    const uint32_t c = big_list[q], n = count[c], s0 = start[c], m = pow2_at_least(n);
+    uint32_t* b = m <= kBlockSortMax ? sbuf : scratch + 2 * (size_t)s0;
+    for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) b[k] = k < n ? slot[s0 + k] : 0xffffffffu;
+    __syncthreads();
+    if (m <= kBlockSortMax)
+      bitonic(b, m, threadIdx.x, blockDim.x, [] { __syncthreads(); });
+    else
+      bitonic(b, m, threadIdx.x, blockDim.x, [] {
+        __threadfence_block();
+        __syncthreads();
+      });
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) slot[s0 + k] = b[k];
+    __syncthreads();
+  }
+}
+
 __global__ void __launch_bounds__(kBlock)
 k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
         const float4* __restrict__ pos, const float4* __restrict__ vel,
@@ -107,7 +193,16 @@ k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   if (i >= N) return;
   const uint32_t c = key[i], s0 = start[c], n = count[c], me = id[i];
   uint32_t r = 0;
-  for (uint32_t j = s0; j < s0 + n; ++j) r += slot[j] < me;
+  if (n <= kLinearRank) {
+    for (uint32_t j = s0; j < s0 + n; ++j) r += slot[j] < me;
+  } else {  // sorted segment: number of smaller ids by binary search
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (slot[s0 + mid] < me) lo = mid + 1; else hi = mid;
+    }
+    r = lo;
+  }
   const uint32_t dest = s0 + r;
   const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
   const float4 x4 = pos[i], v4 = vel[i];
@@ -215,13 +310,33 @@ k_density(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, i
   pres_out[i] = __fmul_rn(__fsub_rn(dens, p.restDensity), p.stiffness);
 }
 
-template <bool kMask, int kThreads, int kMinBlocks>
+// Learned-corrector features of particle i (SPH_MLP_IN = 16), from the
+// neighbours the force pass visits with r < h, weight w = ((h - r)/h)^2:
+//   0 rho/rho0 - 1            1 p / (rho0 g h)          2 neighbours / 64
+//   3 dt/h sum w (v_j - v_i).(x_i - x_j)/r               (velocity divergence)
+//   4-6 dt/h sum w (v_j - v_i) / sum w                   (relative velocity moment)
+//   7-9 sum w (x_j - x_i)/h / sum w                      (position moment)
+//   10-12 SPH velocity increment / (g dt)
+//   13-15 soft-wall velocity increment boundary() gives at the current
+//         position and velocity, / (g dt)   (the stiff wall term is where
+//         a 4x step departs most from four small ones)
+// Written raw (FP32) and/or standardised ((f - mean) * inv_std) in BF16.
+struct FeatAcc {
+  float sw = 0.f, n = 0.f, div = 0.f, rv[3] = {0.f, 0.f, 0.f}, rx[3] = {0.f, 0.f, 0.f};
+};
+struct FeatOut {
+  float* raw;               // N x 16 FP32 or null
+  uint16_t* norm;           // N x 16 BF16 or null
+  const float* stats;       // mean[16], inv_std[16]
+};
+
+template <bool kMask, int kThreads, int kMinBlocks, bool kFeat>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
 k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
         const float4* __restrict__ pos, const float4* __restrict__ vel,
         const float* __restrict__ dens, const float* __restrict__ pres,
         const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
-        const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out) {
+        const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out, FeatOut fo) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
@@ -235,13 +350,31 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   const uint32_t maxpc = p.maxParInCell;
   const int x0 = max(cx - 1, 0), x1 = min(cx + 1, gx - 1);
   float3 F = make_float3(0.f, 0.f, 0.f);
+  FeatAcc fa;
   auto pair = [&](uint32_t j, float3& cell) {
     const float4 xj = __ldg(pos + j);
     const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
     const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
-    if (!(dist2 >= k.h2_out))
-      force_pair_near(k, vi, di, pi, __ldg(vel + j), __ldg(dens + j), __ldg(pres + j), rx, ry, rz,
-                      dist2, cell);
+    if (!(dist2 >= k.h2_out)) {
+      const float4 vj = __ldg(vel + j);
+      force_pair_near(k, vi, di, pi, vj, __ldg(dens + j), __ldg(pres + j), rx, ry, rz, dist2, cell);
+      if (kFeat) {
+        const float r = fmaxf(k.minDist, sqrtf(dist2));
+        if (r < k.h) {
+          const float q = (k.h - r) / k.h, w = q * q;
+          const float dvx = vj.x - vi.x, dvy = vj.y - vi.y, dvz = vj.z - vi.z;
+          fa.sw += w;
+          fa.n += 1.f;
+          fa.div += w * (dvx * rx + dvy * ry + dvz * rz) / r;
+          fa.rv[0] += w * dvx;
+          fa.rv[1] += w * dvy;
+          fa.rv[2] += w * dvz;
+          fa.rx[0] -= w * rx;
+          fa.rx[1] -= w * ry;
+          fa.rx[2] -= w * rz;
+        }
+      }
+    }
   };
   float3 cell = make_float3(0.f, 0.f, 0.f);
   auto flush = [&]() {
@@ -311,6 +444,68 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   const float3 add = velocity_increment(p, F, xi, vi);
   vel_out[i] = make_float4(__fadd_rn(vi.x, add.x), __fadd_rn(vi.y, add.y), __fadd_rn(vi.z, add.z),
                            __fadd_rn(vi.w, 0.f));
+  if (kFeat) {
+    const float dt = p.timeStep, h = p.h;
+    const float g = sqrtf(p.gravity.x * p.gravity.x + p.gravity.y * p.gravity.y +
+                          p.gravity.z * p.gravity.z) + 1e-6f;
+    const float s = __fmul_rn(p.particleMass, p.timeStep), isw = 1.f / (fa.sw + 1e-6f);
+    float f[16];
+    f[0] = di / p.restDensity - 1.f;
+    f[1] = pi / (p.restDensity * g * h);
+    f[2] = fa.n * (1.f / 64.f);
+    f[3] = fa.div * dt / h;
+    f[4] = fa.rv[0] * isw * dt / h;
+    f[5] = fa.rv[1] * isw * dt / h;
+    f[6] = fa.rv[2] * isw * dt / h;
+    f[7] = fa.rx[0] * isw / h;
+    f[8] = fa.rx[1] * isw / h;
+    f[9] = fa.rx[2] * isw / h;
+    f[10] = F.x * s / (g * dt);
+    f[11] = F.y * s / (g * dt);
+    f[12] = F.z * s / (g * dt);
+    {
+      float3 bx = make_float3(xi.x, xi.y, xi.z), bv = make_float3(vi.x, vi.y, vi.z);
+      boundary(p, bx, bv);
+      f[13] = (bv.x - vi.x) / (g * dt);
+      f[14] = (bv.y - vi.y) / (g * dt);
+      f[15] = (bv.z - vi.z) / (g * dt);
+    }
+    if (fo.raw) {
+      float4* o = reinterpret_cast<float4*>(fo.raw + (size_t)i * 16);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) o[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+    }
+    if (fo.norm) {
+      uint32_t u[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float a = (f[2 * q] - fo.stats[2 * q]) * fo.stats[16 + 2 * q];
+        const float b = (f[2 * q + 1] - fo.stats[2 * q + 1]) * fo.stats[16 + 2 * q + 1];
+        __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+        u[q] = *reinterpret_cast<uint32_t*>(&v);
+      }
+      uint4* o = reinterpret_cast<uint4*>(fo.norm + (size_t)i * 16);
+      o[0] = make_uint4(u[0], u[1], u[2], u[3]);
+      o[1] = make_uint4(u[4], u[5], u[6], u[7]);
+    }
+  }
+}
+
+// vel[i] += y[i] * out_scale * g * dt (the MLP's correction, sorted order).
+__global__ void k_apply_correction(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff,
+                                   int S, uint32_t N, const float* __restrict__ y,
+                                   const float* __restrict__ out_scale, float4* __restrict__ vel) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const SimParams& p = sc[S == 1 ? 0 : scene_of(poff, S, i)].p;
+  const float g = sqrtf(p.gravity.x * p.gravity.x + p.gravity.y * p.gravity.y +
+                        p.gravity.z * p.gravity.z) + 1e-6f;
+  const float u = g * p.timeStep;
+  float4 v = vel[i];
+  v.x += y[3 * i + 0] * out_scale[0] * u;
+  v.y += y[3 * i + 1] * out_scale[1] * u;
+  v.z += y[3 * i + 2] * out_scale[2] * u;
+  vel[i] = v;
 }
 
 // ---- buffer API kernels ---------------------------------------------------
@@ -412,6 +607,8 @@ struct SphSystem {
   float4* vel[2] = {nullptr, nullptr};
   uint32_t* id[2] = {nullptr, nullptr};
   uint32_t *key = nullptr, *rank = nullptr, *slot = nullptr;
+  uint32_t *big_list = nullptr, *big_count = nullptr, *sort_scratch = nullptr;
+  unsigned big_blocks = 1;
   uint32_t *count = nullptr, *start = nullptr, *scan_tmp = nullptr;
   float *dens = nullptr, *pres = nullptr;
   unsigned long long* masks = nullptr;  // kRows x N neighbour masks (null: walks without)
@@ -427,6 +624,17 @@ struct SphSystem {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // graph_steps steps, keyed by cp at launch
   uint32_t graph_steps = 2;                         // steps per captured graph (even)
   int walk_shape = kDefaultShape;                   // index into kWalkBlocks
+  // learned corrector
+  SceneDesc* d_coarse = nullptr;     // scene table with timeStep * coarse_sub
+  uint32_t coarse_sub = 0;
+  void* mlp_img = nullptr;           // packed BF16 weights
+  float* mlp_aux = nullptr;          // feature mean[16], inv_std[16], out_scale[3]
+  bool model_set = false;
+  uint16_t* feat = nullptr;          // N x 16 standardised features (BF16)
+  float* mlp_y = nullptr;            // N x 3 corrections
+  float4* bk_pos = nullptr;          // checkpoint for the fallback
+  float4* bk_vel = nullptr;
+  uint32_t* bk_id = nullptr;
 };
 
 namespace {
@@ -454,31 +662,48 @@ void drop_graphs(SphSystem* s) {
     }
 }
 
+// What one enqueued step uses besides the handle's buffers.
+struct StepOpts {
+  const SceneDesc* scenes = nullptr;  // scene table (fine or coarse time step)
+  bool feat = false;                  // force pass also writes learned-corrector features
+  FeatOut fo = {nullptr, nullptr, nullptr};
+};
+
 template <bool kMask, int kThreads, int kMinBlocks, class Mark>
-void launch_walks_shape(SphSystem* s, cudaStream_t st, int b, int v, Mark& mark) {
+void launch_walks_shape(SphSystem* s, cudaStream_t st, int b, int v, const StepOpts& o, Mark& mark) {
   const unsigned g = grid_for(s->N, kThreads);
   k_density<kMask, kThreads, kMinBlocks><<<g, kThreads, 0, st>>>(
-      s->d_scenes, s->d_poff, s->S, s->N, s->pos[b], s->start, s->count, s->dens, s->pres,
+      o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->start, s->count, s->dens, s->pres,
       s->masks, s->flags);
   mark();
-  k_force<kMask, kThreads, kMinBlocks><<<g, kThreads, 0, st>>>(
-      s->d_scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->pres, s->start,
-      s->count, s->masks, s->vel[v]);
+  if (o.feat)
+    k_force<kMask, kThreads, kMinBlocks, true><<<g, kThreads, 0, st>>>(
+        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->pres, s->start,
+        s->count, s->masks, s->vel[v], o.fo);
+  else
+    k_force<kMask, kThreads, kMinBlocks, false><<<g, kThreads, 0, st>>>(
+        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->pres, s->start,
+        s->count, s->masks, s->vel[v], o.fo);
 }
 
 template <bool kMask, class Mark>
-void launch_walks(SphSystem* s, cudaStream_t st, int b, int v, Mark& mark) {
+void launch_walks(SphSystem* s, cudaStream_t st, int b, int v, const StepOpts& o, Mark& mark) {
   switch (s->walk_shape) {
-    case 0: launch_walks_shape<kMask, 64, 8>(s, st, b, v, mark); break;
-    case 2: launch_walks_shape<kMask, 256, 2>(s, st, b, v, mark); break;
-    default: launch_walks_shape<kMask, 128, 4>(s, st, b, v, mark); break;
+    case 0: launch_walks_shape<kMask, 64, 8>(s, st, b, v, o, mark); break;
+    case 2: launch_walks_shape<kMask, 256, 2>(s, st, b, v, o, mark); break;
+    default: launch_walks_shape<kMask, 128, 4>(s, st, b, v, o, mark); break;
   }
 }
 
 // Enqueues one step on `st`, advancing s->cp.  With `ev` (kStepStages + 1
 // events) an event is recorded before the first stage and after each one.
 constexpr int kStepStages = 6;
-int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr,
+                 const StepOpts* opts = nullptr) {
+  StepOpts o;
+  if (opts) o = *opts;
+  if (!o.scenes) o.scenes = s->d_scenes;
+  const SceneDesc* sc = o.scenes;
   const unsigned gN = grid_for(s->N, kBlock);
   const int a = s->cp, b = 1 - s->cp, v = s->cv;
   int e = 0;
@@ -487,21 +712,26 @@ int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
   };
   mark();
   SPH_CUDA(cudaMemsetAsync(s->count, 0, sizeof(uint32_t) * s->C, st), "step: clear counts");
-  k_integrate_count<<<gN, kBlock, 0, st>>>(s->d_scenes, s->d_poff, s->S, s->N, s->pos[a], s->vel[v],
+  k_integrate_count<<<gN, kBlock, 0, st>>>(sc, s->d_poff, s->S, s->N, s->pos[a], s->vel[v],
                                            s->key, s->rank, s->count, s->flags);
   mark();
   SPH_TRY(exclusive_scan(s->count, s->start, s->C, s->scan_tmp, st));
   mark();
   k_scatter_ids<<<gN, kBlock, 0, st>>>(s->N, s->key, s->rank, s->id[a], s->start, s->slot);
+  SPH_CUDA(cudaMemsetAsync(s->big_count, 0, sizeof(uint32_t), st), "step: clear big-cell count");
+  k_sort_cells<<<grid_for(s->C, kSortWarps), kSortWarps * 32, 0, st>>>(
+      s->C, s->start, s->count, s->slot, s->big_list, s->big_count);
+  k_sort_big_cells<<<s->big_blocks, kBigThreads, kBlockSortMax * sizeof(uint32_t), st>>>(
+      s->start, s->count, s->slot, s->big_list, s->big_count, s->sort_scratch);
   mark();
-  k_place<<<gN, kBlock, 0, st>>>(s->d_scenes, s->d_poff, s->S, s->N, s->pos[a], s->vel[v], s->id[a],
+  k_place<<<gN, kBlock, 0, st>>>(sc, s->d_poff, s->S, s->N, s->pos[a], s->vel[v], s->id[a],
                                  s->key, s->start, s->count, s->slot, s->pos[b], s->vel[1 - v],
                                  s->id[b]);
   mark();
   if (s->masks)
-    launch_walks<true>(s, st, b, v, mark);
+    launch_walks<true>(s, st, b, v, o, mark);
   else
-    launch_walks<false>(s, st, b, v, mark);
+    launch_walks<false>(s, st, b, v, o, mark);
   mark();
   SPH_CUDA(cudaGetLastError(), "step kernels");
   s->cp = b;
@@ -533,7 +763,9 @@ void free_all(SphSystem* s) {
   drop_graphs(s);
   void* bufs[] = {s->d_scenes, s->d_poff, s->d_coff, s->pos[0], s->pos[1], s->vel[0], s->vel[1],
                   s->id[0], s->id[1], s->key, s->rank, s->slot, s->count, s->start, s->scan_tmp,
-                  s->dens, s->pres, s->masks, s->flags, s->stats, s->staging};
+                  s->dens, s->pres, s->masks, s->flags, s->stats, s->staging, s->d_coarse,
+                  s->mlp_img, s->mlp_aux, s->feat, s->mlp_y, s->bk_pos, s->bk_vel, s->bk_id,
+                  s->big_list, s->big_count, s->sort_scratch};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
@@ -583,6 +815,9 @@ int create(const SimParams* scenes, uint32_t count, SphSystem** out) {
   ALLOC(s->key, n, "cell keys");
   ALLOC(s->rank, n, "cell ranks");
   ALLOC(s->slot, n, "cell slots");
+  ALLOC(s->big_list, n / (kWarpSortMax + 1) + 1, "crowded-cell list");
+  ALLOC(s->big_count, 1, "crowded-cell count");
+  ALLOC(s->sort_scratch, 2 * n, "cell sort scratch");
   ALLOC(s->count, c, "cell counts");
   ALLOC(s->start, c, "cell starts");
   ALLOC(s->scan_tmp, scan_scratch_words(c), "scan scratch");
@@ -596,6 +831,16 @@ int create(const SimParams* scenes, uint32_t count, SphSystem** out) {
 #undef ALLOC
   if (rc == SPH_OK) rc = cuda_check(cudaStreamCreate(&s->stream), "stream");
   s->own_stream = rc == SPH_OK;
+  if (rc == SPH_OK)
+    rc = cuda_check(cudaFuncSetAttribute(k_sort_big_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(kBlockSortMax * sizeof(uint32_t))),
+                    "crowded-cell sort shared memory");
+  if (rc == SPH_OK) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    s->big_blocks = (unsigned)(sms > 0 ? sms : 1);
+  }
   if (rc == SPH_OK) {
     for (int k = 0; k < 2; ++k) {
       cudaMemsetAsync(s->pos[k], 0, sizeof(float4) * n, s->stream);
@@ -818,6 +1063,130 @@ int sph_autotune(SphSystem* s, uint32_t trial_steps, float* ms_per_step, uint32_
   if (sv) cudaFree(sv);
   if (si) cudaFree(si);
   return rc;
+}
+
+namespace {
+
+// Scene table whose time step is `sub` times the scenes' own.
+int ensure_coarse(SphSystem* s, uint32_t sub) {
+  if (!s->d_coarse) SPH_TRY(dalloc(&s->d_coarse, s->S, "coarse scene table"));
+  std::vector<SceneDesc> h(s->S);
+  for (int i = 0; i < s->S; ++i) {
+    h[i].p = s->params[i];
+    h[i].p.timeStep = s->params[i].timeStep * (float)sub;
+    h[i].p_off = s->poff[i];
+    h[i].p_cnt = s->poff[i + 1] - s->poff[i];
+    h[i].c_off = s->coff[i];
+    h[i].c_cnt = s->coff[i + 1] - s->coff[i];
+  }
+  SPH_CUDA(cudaMemcpyAsync(s->d_coarse, h.data(), sizeof(SceneDesc) * s->S, cudaMemcpyHostToDevice,
+                           s->stream),
+           "coarse scene table");
+  SPH_CUDA(cudaStreamSynchronize(s->stream), "coarse scene table");
+  s->coarse_sub = sub;
+  return SPH_OK;
+}
+
+// Per-scene mean density of the last step and non-finite counts (host).
+int scene_stats(SphSystem* s, std::vector<double>& out) {
+  out.assign(4 * s->S, 0.0);
+  return sph_stats(s, out.data());
+}
+
+}  // namespace
+
+int sph_learned_set_model(SphSystem* s, const float* params, const float* feat_stats,
+                          const float* out_scale) {
+  if (!s || !params || !feat_stats || !out_scale) return fail(SPH_ERR_ARG, "set_model: null argument");
+  const int np = sph_mlp_param_count();
+  float* dprm = nullptr;
+  SPH_TRY(dalloc(&dprm, np, "model parameters"));
+  if (!s->mlp_img) SPH_TRY(dalloc((uint8_t**)&s->mlp_img, sph_mlp_packed_bytes(), "packed model"));
+  if (!s->mlp_aux) SPH_TRY(dalloc(&s->mlp_aux, 35, "model statistics"));
+  int rc = cuda_check(cudaMemcpyAsync(dprm, params, sizeof(float) * np, cudaMemcpyHostToDevice,
+                                      s->stream), "model upload");
+  if (rc == SPH_OK) rc = cuda_check(cudaMemcpyAsync(s->mlp_aux, feat_stats, sizeof(float) * 32,
+                                                    cudaMemcpyHostToDevice, s->stream), "model upload");
+  if (rc == SPH_OK) rc = cuda_check(cudaMemcpyAsync(s->mlp_aux + 32, out_scale, sizeof(float) * 3,
+                                                    cudaMemcpyHostToDevice, s->stream), "model upload");
+  if (rc == SPH_OK) rc = sph_mlp_pack(dprm, s->mlp_img, s->stream);
+  if (rc == SPH_OK) rc = cuda_check(cudaStreamSynchronize(s->stream), "model upload");
+  cudaFree(dprm);
+  s->model_set = rc == SPH_OK;
+  return rc;
+}
+
+int sph_features_step(SphSystem* s, uint32_t substeps, float* feat_raw, uint32_t* ids) {
+  if (!s || substeps == 0) return fail(SPH_ERR_ARG, "features_step: bad arguments");
+  if (s->coarse_sub != substeps) SPH_TRY(ensure_coarse(s, substeps));
+  StepOpts o;
+  o.scenes = s->d_coarse;
+  o.feat = true;
+  o.fo = {feat_raw, nullptr, nullptr};
+  SPH_TRY(enqueue_step(s, s->stream, nullptr, &o));
+  if (ids)
+    SPH_CUDA(cudaMemcpyAsync(ids, s->id[s->cp], sizeof(uint32_t) * s->N, cudaMemcpyDeviceToDevice,
+                             s->stream), "features_step ids");
+  return SPH_OK;
+}
+
+int sph_learned_step(SphSystem* s, uint32_t coarse_steps, uint32_t substeps, float tol,
+                     uint32_t* fallbacks) {
+  if (!s || substeps == 0) return fail(SPH_ERR_ARG, "learned_step: bad arguments");
+  if (!s->model_set) return fail(SPH_ERR_STATE, "learned_step: no model (sph_learned_set_model)");
+  if (s->coarse_sub != substeps) SPH_TRY(ensure_coarse(s, substeps));
+  if (!s->feat) SPH_TRY(dalloc(&s->feat, (size_t)16 * s->N, "features"));
+  if (!s->mlp_y) SPH_TRY(dalloc(&s->mlp_y, (size_t)3 * s->N, "corrections"));
+  if (!s->bk_pos) SPH_TRY(dalloc(&s->bk_pos, s->N, "checkpoint"));
+  if (!s->bk_vel) SPH_TRY(dalloc(&s->bk_vel, s->N, "checkpoint"));
+  if (!s->bk_id) SPH_TRY(dalloc(&s->bk_id, s->N, "checkpoint"));
+  std::vector<double> st, ref;
+  bool have_ref = false;
+  if (s->stepped) {
+    SPH_TRY(scene_stats(s, ref));
+    have_ref = true;
+  }
+  uint32_t fb = 0;
+  StepOpts o;
+  o.scenes = s->d_coarse;
+  o.feat = true;
+  o.fo = {nullptr, s->feat, s->mlp_aux};
+  for (uint32_t k = 0; k < coarse_steps; ++k) {
+    const int cp0 = s->cp, cv0 = s->cv;
+    SPH_CUDA(cudaMemcpyAsync(s->bk_pos, s->pos[cp0], sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream), "checkpoint");
+    SPH_CUDA(cudaMemcpyAsync(s->bk_vel, s->vel[cv0], sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream), "checkpoint");
+    SPH_CUDA(cudaMemcpyAsync(s->bk_id, s->id[cp0], sizeof(uint32_t) * s->N, cudaMemcpyDeviceToDevice, s->stream), "checkpoint");
+    SPH_TRY(enqueue_step(s, s->stream, nullptr, &o));
+    SPH_TRY(sph_mlp_forward(s->mlp_img, s->feat, s->N, s->mlp_y, s->stream));
+    k_apply_correction<<<grid_for(s->N, kBlock), kBlock, 0, s->stream>>>(
+        s->d_coarse, s->d_poff, s->S, s->N, s->mlp_y, s->mlp_aux + 32, s->vel[s->cv]);
+    SPH_CUDA(cudaGetLastError(), "apply correction");
+    // density-deviation check: every scene's mean density may move by at
+    // most `tol` (relative) over the coarse step, and nothing may be NaN/Inf
+    SPH_TRY(scene_stats(s, st));
+    bool ok = true;
+    for (int i = 0; i < s->S && ok; ++i) {
+      if (st[4 * i + 3] != 0.0 || !(st[4 * i + 1] == st[4 * i + 1])) ok = false;
+      if (have_ref && ok) {
+        const double r0 = ref[4 * i + 1];
+        if (!(fabs(st[4 * i + 1] - r0) <= tol * r0)) ok = false;
+      }
+    }
+    if (!ok) {  // fall back: restore and take `substeps` fine steps
+      ++fb;
+      s->cp = cp0;
+      s->cv = cv0;
+      SPH_CUDA(cudaMemcpyAsync(s->pos[cp0], s->bk_pos, sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream), "restore");
+      SPH_CUDA(cudaMemcpyAsync(s->vel[cv0], s->bk_vel, sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream), "restore");
+      SPH_CUDA(cudaMemcpyAsync(s->id[cp0], s->bk_id, sizeof(uint32_t) * s->N, cudaMemcpyDeviceToDevice, s->stream), "restore");
+      for (uint32_t q = 0; q < substeps; ++q) SPH_TRY(enqueue_step(s, s->stream));
+      SPH_TRY(scene_stats(s, st));
+    }
+    ref = st;
+    have_ref = true;
+  }
+  if (fallbacks) *fallbacks = fb;
+  return SPH_OK;
 }
 
 int sph_step_timed(SphSystem* s, float* stage_ms, uint32_t nstages) {

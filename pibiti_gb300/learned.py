@@ -1,0 +1,293 @@
+"""The learned corrector: training data, training and evaluation.
+
+A coarse step is one SPH step with the time step multiplied by SUBSTEPS (4);
+its force pass also writes 16 features per particle (density, pressure,
+neighbour count, velocity divergence, kernel-weighted relative velocity and
+position moments, SPH velocity increment, soft-wall velocity increment).  The MLP (16 -> 64 -> 64 -> 3,
+BF16 tensor-core kernels in csrc/sph_mlp.cu) predicts the difference between
+SUBSTEPS plain steps of dt and the coarse step, as a velocity correction in
+units of |g| dt_coarse.
+
+Training data comes from the batched ensemble (configs.ensemble): from a state
+of the fine-dt run, one featured coarse step and SUBSTEPS fine steps give one
+(features, target) pair per particle.  Training runs the project's own
+forward/backward kernels (sph_mlp_train_pass) with Adam (sph_mlp_adam).
+Device buffers are torch tensors passed by pointer.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .sph import ARRAY_POS, ARRAY_VEL, SPH, Scene
+
+SUBSTEPS = 4
+HERE = os.path.dirname(os.path.abspath(__file__))
+MODEL_PATH = os.path.join(HERE, "models", "corrector.npz")
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+@dataclass
+class Model:
+    params: np.ndarray      # 5443 FP32
+    feat_mean: np.ndarray   # 16
+    feat_std: np.ndarray    # 16
+    out_scale: np.ndarray   # 3
+    info: dict
+
+    def save(self, path: str = MODEL_PATH) -> None:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        np.savez(path, params=self.params, feat_mean=self.feat_mean, feat_std=self.feat_std,
+                 out_scale=self.out_scale, info=np.array(repr(self.info)))
+
+    @classmethod
+    def load(cls, path: str = MODEL_PATH) -> "Model":
+        with np.load(path, allow_pickle=False) as z:
+            return cls(z["params"].astype(np.float32), z["feat_mean"].astype(np.float32),
+                       z["feat_std"].astype(np.float32), z["out_scale"].astype(np.float32),
+                       {"saved": str(z["info"])})
+
+    def install(self, sph: SPH) -> None:
+        stats = np.concatenate([self.feat_mean, 1.0 / self.feat_std]).astype(np.float32)
+        prm = np.ascontiguousarray(self.params, np.float32)
+        osc = np.ascontiguousarray(self.out_scale, np.float32)
+        _lib.check(_lib.lib().sph_learned_set_model(
+            sph._h, ctypes.c_void_p(prm.ctypes.data), ctypes.c_void_p(stats.ctypes.data),
+            ctypes.c_void_p(osc.ctypes.data)))
+
+
+def learned_step(sph: SPH, coarse_steps: int, substeps: int = SUBSTEPS, tol: float = 0.01) -> int:
+    """Coarse steps with the MLP correction; returns the number of fallbacks."""
+    fb = ctypes.c_uint32()
+    _lib.check(_lib.lib().sph_learned_step(sph._h, coarse_steps, substeps, tol, ctypes.byref(fb)))
+    return fb.value
+
+
+def features_step(sph: SPH, feat, ids, substeps: int = SUBSTEPS) -> None:
+    _lib.check(_lib.lib().sph_features_step(sph._h, substeps, _p(feat), _p(ids)))
+
+
+def _g_dt(params_list, sizes, substeps, torch):
+    vals = []
+    for p, n in zip(params_list, sizes):
+        g = float(np.sqrt(p.gravity.x ** 2 + p.gravity.y ** 2 + p.gravity.z ** 2)) + 1e-6
+        vals.append(np.full(n, g * p.timeStep * substeps, np.float32))
+    return torch.from_numpy(np.concatenate(vals)).cuda()
+
+
+def generate(xmls, pos, vel, sizes, snapshots: int = 8, warm: int = 20, gap: int = 20,
+             substeps: int = SUBSTEPS):
+    """(features [M,16], targets [M,3]) on the GPU from `snapshots` states of
+    the fine-dt run of the given scenes."""
+    import torch
+    ps = [Scene.parse(x).params for x in xmls]
+    fine, coarse = SPH(ps), SPH(ps)
+    fine.set_array(ARRAY_POS, pos)
+    fine.set_array(ARRAY_VEL, vel)
+    fine.update(warm)
+    n = fine.n
+    gdt = _g_dt(ps, sizes, substeps, torch)
+    tp = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    tv = torch.empty_like(tp)
+    vc = torch.empty_like(tp)
+    vf = torch.empty_like(tp)
+    feats, targets = [], []
+    for _ in range(snapshots):
+        fine.get_array(ARRAY_POS, tp)
+        fine.get_array(ARRAY_VEL, tv)
+        torch.cuda.synchronize()
+        coarse.set_array(ARRAY_POS, tp)
+        coarse.set_array(ARRAY_VEL, tv)
+        f = torch.empty((n, 16), dtype=torch.float32, device="cuda")
+        ids = torch.empty(n, dtype=torch.int32, device="cuda")
+        features_step(coarse, f, ids, substeps)
+        coarse.get_array(ARRAY_VEL, vc)
+        fine.update(substeps)
+        fine.get_array(ARRAY_VEL, vf)
+        torch.cuda.synchronize()
+        t = (vf - vc)[:, :3] / gdt[:, None]
+        idx = ids.long()
+        feats.append(f)
+        targets.append(t[idx].contiguous())
+        fine.update(gap)
+    fine.close()
+    coarse.close()
+    return torch.cat(feats), torch.cat(targets)
+
+
+def train(feats, targets, epochs: int = 6, batch: int = 65536, lr: float = 2e-3, seed: int = 0,
+          log=None) -> Model:
+    """Adam on the project's MLP kernels; returns the trained model."""
+    import torch
+    L = _lib.lib()
+    mean = feats.mean(0)
+    std = feats.std(0) + 1e-6
+    x = ((feats - mean) / std).to(torch.bfloat16).view(torch.int16).contiguous()
+    out_scale = targets.std(0) + 1e-9
+    # the rare very large targets (stiff wall contacts) are clipped at 4 sigma
+    t = (targets / out_scale).clamp(-4.0, 4.0).contiguous()
+    rng = np.random.default_rng(seed)
+    parts = []
+    for k_in, k_out in ((16, 64), (64, 64), (64, 3)):
+        parts.append(rng.normal(0, 1.0 / np.sqrt(k_in), size=(k_in, k_out)).ravel())
+        parts.append(np.zeros(k_out))
+    prm = torch.from_numpy(np.concatenate(parts).astype(np.float32)).cuda()
+    m, v, grad = torch.zeros_like(prm), torch.zeros_like(prm), torch.zeros_like(prm)
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    img = torch.zeros(L.sph_mlp_packed_bytes(), dtype=torch.uint8, device="cuda")
+    _lib.check(L.sph_mlp_pack(_p(prm), _p(img), None))
+    n = x.shape[0]
+    step = 0
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    history = []
+    for ep in range(epochs):
+        perm = torch.randperm(n, device="cuda", generator=gen)
+        lr_ep = lr * (0.5 ** max(0, ep - epochs // 2))
+        tot, cnt = 0.0, 0
+        for b0 in range(0, n - batch + 1, batch):
+            idx = perm[b0:b0 + batch]
+            xb, tb = x[idx].contiguous(), t[idx].contiguous()
+            grad.zero_()
+            loss.zero_()
+            _lib.check(L.sph_mlp_train_pass(_p(img), _p(xb), _p(tb), batch, _p(grad), _p(loss), None))
+            step += 1
+            _lib.check(L.sph_mlp_adam(_p(prm), _p(m), _p(v), _p(grad), lr_ep, 0.9, 0.999, 1e-8,
+                                      step, None))
+            _lib.check(L.sph_mlp_pack(_p(prm), _p(img), None))
+            tot += loss.item()
+            cnt += 1
+        history.append(tot / max(cnt, 1))
+        if log:
+            log(f"epoch {ep}: mean loss {history[-1]:.4f}")
+    return Model(prm.cpu().numpy(), mean.cpu().numpy(), std.cpu().numpy(),
+                 out_scale.cpu().numpy(), {"loss_history": history, "samples": int(n)})
+
+
+def one_step_errors(model: Model, xml: str, pos, vel, warm: int = 40,
+                    substeps: int = SUBSTEPS) -> dict:
+    """Velocity error of one coarse step, with and without the network,
+    against `substeps` fine steps from the same state (mean |dv| over
+    particles, in m/s)."""
+    import torch
+    p = Scene.parse(xml).params
+    with SPH(p) as fine, SPH(p) as plain, SPH(p) as lrn:
+        fine.set_array(ARRAY_POS, pos)
+        fine.set_array(ARRAY_VEL, vel)
+        fine.update(warm)
+        s_pos, s_vel = fine.get_array(ARRAY_POS), fine.get_array(ARRAY_VEL)
+        for h in (plain, lrn):
+            h.set_array(ARRAY_POS, s_pos)
+            h.set_array(ARRAY_VEL, s_vel)
+        fine.update(substeps)
+        f = torch.empty((fine.n, 16), dtype=torch.float32, device="cuda")
+        ids = torch.empty(fine.n, dtype=torch.int32, device="cuda")
+        features_step(plain, f, ids, substeps)
+        model.install(lrn)
+        fb = learned_step(lrn, 1, substeps, tol=1e9)
+        vf, vp, vl = fine.get_array(ARRAY_VEL), plain.get_array(ARRAY_VEL), lrn.get_array(ARRAY_VEL)
+    e_plain = float(np.abs(vp[:, :3] - vf[:, :3]).sum(1).mean())
+    e_learned = float(np.abs(vl[:, :3] - vf[:, :3]).sum(1).mean())
+    return {"coarse_plain": e_plain, "coarse_learned": e_learned, "fallbacks": fb}
+
+
+def rollout(model: Model, xml: str, pos, vel, fine_steps: int, substeps: int = SUBSTEPS,
+            tol: float = 0.01, warm: int = 0) -> dict:
+    """Mean-density trajectories of the fine-dt plain run, the coarse run
+    without the network and the learned run, sampled every `substeps` fine
+    steps; errors relative to the fine run, and the wall time of each."""
+    import torch
+    p = Scene.parse(xml).params
+    pc = p.copy()
+    pc.timeStep = p.timeStep * substeps
+    coarse_steps = fine_steps // substeps
+    out = {}
+    with SPH(p) as fine:
+        fine.set_array(ARRAY_POS, pos)
+        fine.set_array(ARRAY_VEL, vel)
+        if warm:
+            fine.update(warm)
+        s_pos, s_vel = fine.get_array(ARRAY_POS), fine.get_array(ARRAY_VEL)
+        rho_f = []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(coarse_steps):
+            fine.update(substeps)
+            rho_f.append(fine.stats()[0][1])
+        out["fine_s"] = time.perf_counter() - t0
+    with SPH(pc) as c:
+        c.set_array(ARRAY_POS, s_pos)
+        c.set_array(ARRAY_VEL, s_vel)
+        rho_c = []
+        for _ in range(coarse_steps):
+            c.update(1)
+            rho_c.append(c.stats()[0][1])
+    with SPH(p) as lrn:
+        lrn.set_array(ARRAY_POS, s_pos)
+        lrn.set_array(ARRAY_VEL, s_vel)
+        model.install(lrn)
+        rho_l, fb = [], 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(coarse_steps):
+            fb += learned_step(lrn, 1, substeps, tol)
+            rho_l.append(lrn.stats()[0][1])
+        out["learned_s"] = time.perf_counter() - t0
+    rho_f, rho_c, rho_l = map(np.asarray, (rho_f, rho_c, rho_l))
+    out.update({
+        "err_coarse_plain": float(np.max(np.abs(rho_c - rho_f) / rho_f)),
+        "err_learned": float(np.max(np.abs(rho_l - rho_f) / rho_f)),
+        "fallbacks": int(fb), "coarse_steps": coarse_steps,
+        "rho_fine_end": float(rho_f[-1]), "rho_learned_end": float(rho_l[-1]),
+    })
+    return out
+
+
+def main(argv=None) -> int:
+    """python -m pibiti_gb300.learned train|evaluate [--scenes S] ..."""
+    import argparse
+    import json
+    import sys
+    import torch
+    from . import configs
+    ap = argparse.ArgumentParser()
+    ap.add_argument("cmd", choices=["train", "evaluate"])
+    ap.add_argument("--scenes", type=int, default=256)
+    ap.add_argument("--snapshots", type=int, default=6)
+    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--fine-steps", type=int, default=400)
+    ap.add_argument("--model", default=MODEL_PATH)
+    a = ap.parse_args(argv)
+    log = lambda *m: print(*m, file=sys.stderr, flush=True)  # noqa: E731
+    torch.cuda.set_device(0)
+    if a.cmd == "train":
+        e = configs.ensemble(scenes=a.scenes)
+        t0 = time.perf_counter()
+        f, t = generate(e.xmls, e.pos, e.vel, e.sizes, snapshots=a.snapshots)
+        log(f"generated {f.shape[0]} samples in {time.perf_counter() - t0:.1f} s")
+        t0 = time.perf_counter()
+        model = train(f, t, epochs=a.epochs, log=log)
+        model.info.update({"scenes": a.scenes, "snapshots": a.snapshots, "epochs": a.epochs,
+                           "train_s": time.perf_counter() - t0})
+        model.save(a.model)
+        w = configs.dambreak_small(side=32)
+        print(json.dumps({"trained": model.info,
+                          "one_step_32k": one_step_errors(model, w.xml, w.pos, w.vel)}))
+    else:
+        model = Model.load(a.model)
+        w = configs.dambreak_double()
+        print(json.dumps({"one_step_1M": one_step_errors(model, w.xml, w.pos, w.vel),
+                          "rollout_1M": rollout(model, w.xml, w.pos, w.vel, a.fine_steps)}))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -1,0 +1,115 @@
+"""The tensor-core MLP kernels (sph_mlp_*) through the C ABI against the
+NumPy oracle (oracle/mlp.py), which rounds to BF16 at the same places.
+
+Tolerances: outputs within 1e-2 of the output scale; each gradient block
+(W1, b1, W2, b2, W3, b3) within 2e-2 relative in the 2-norm; the loss within
+1e-3 relative.  The residual differences come from tanh (device vs double)
+occasionally flipping a BF16 rounding, and from FP32 accumulation order.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import mlp as omlp
+
+pytestmark = pytest.mark.gpu
+
+
+def _lib():
+    from pibiti_gb300 import _lib
+    return _lib, _lib.lib()
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _pack(torch, params):
+    _l, L = _lib()
+    prm = torch.from_numpy(np.asarray(params, np.float32)).cuda()
+    img = torch.zeros(L.sph_mlp_packed_bytes(), dtype=torch.uint8, device="cuda")
+    _l.check(L.sph_mlp_pack(_p(prm), _p(img), None))
+    return prm, img
+
+
+def _x(torch, x):
+    return torch.from_numpy(omlp.bf16_bits(x).view(np.int16).copy()).cuda()
+
+
+def test_sizes(cuda):
+    _l, L = _lib()
+    assert L.sph_mlp_param_count() == omlp.COUNT == 5443
+
+
+@pytest.mark.parametrize("n", [1, 37, 4096, 100_003])
+def test_forward(cuda, n):
+    torch = cuda
+    _l, L = _lib()
+    rng = np.random.default_rng(n)
+    params = omlp.init(3)
+    params[1024:1088] = rng.normal(0, 0.1, 64)  # nonzero biases
+    x = rng.normal(0, 1, size=(n, 16)).astype(np.float32)
+    _, img = _pack(torch, params)
+    y = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
+    _l.check(L.sph_mlp_forward(_p(img), _p(_x(torch, x)), n, _p(y), None))
+    torch.cuda.synchronize()
+    ref, _ = omlp.forward(params, x)
+    scale = max(np.abs(ref).max(), 1e-3)
+    np.testing.assert_allclose(y.cpu().numpy(), ref, rtol=0, atol=1e-2 * scale)
+
+
+@pytest.mark.parametrize("n", [64, 1000, 50_000])
+def test_gradients(cuda, n):
+    torch = cuda
+    _l, L = _lib()
+    rng = np.random.default_rng(7 + n)
+    params = omlp.init(5)
+    params[1024:1088] = rng.normal(0, 0.1, 64)
+    params[5440:5443] = rng.normal(0, 0.1, 3)
+    x = rng.normal(0, 1, size=(n, 16)).astype(np.float32)
+    t = rng.normal(0, 0.5, size=(n, 3)).astype(np.float32)
+    _, img = _pack(torch, params)
+    grad = torch.zeros(omlp.COUNT, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    tt = torch.from_numpy(t).cuda()
+    _l.check(L.sph_mlp_train_pass(_p(img), _p(_x(torch, x)), _p(tt), n, _p(grad), _p(loss), None))
+    torch.cuda.synchronize()
+    ref_loss, ref_g = omlp.loss_and_grad(params, x, t)
+    assert abs(loss.item() - ref_loss) <= 1e-3 * ref_loss
+    g = grad.cpu().numpy().astype(np.float64)
+    o = 0
+    for name, shape in omlp.SIZES:
+        k = int(np.prod(shape))
+        a, b = g[o:o + k], ref_g[o:o + k]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        assert rel <= 2e-2, (name, rel)
+        o += k
+
+
+def test_adam_fits(cuda):
+    """The kernels train: a smooth target is fitted, the loss falls 10x."""
+    torch = cuda
+    _l, L = _lib()
+    rng = np.random.default_rng(0)
+    n = 32768
+    x = rng.normal(0, 1, size=(n, 16)).astype(np.float32)
+    t = np.stack([np.sin(x[:, 0]), 0.5 * x[:, 1] * x[:, 2], np.tanh(x[:, 3] - x[:, 4])], 1)
+    t = t.astype(np.float32)
+    prm, img = _pack(torch, omlp.init(11))
+    m = torch.zeros_like(prm)
+    v = torch.zeros_like(prm)
+    grad = torch.zeros_like(prm)
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    xd, td = _x(torch, x), torch.from_numpy(t).cuda()
+    losses = []
+    for step in range(1, 401):
+        grad.zero_()
+        loss.zero_()
+        _l.check(L.sph_mlp_train_pass(_p(img), _p(xd), _p(td), n, _p(grad), _p(loss), None))
+        _l.check(L.sph_mlp_adam(_p(prm), _p(m), _p(v), _p(grad), 3e-3, 0.9, 0.999, 1e-8, step, None))
+        _l.check(L.sph_mlp_pack(_p(prm), _p(img), None))
+        if step in (1, 400):
+            torch.cuda.synchronize()
+            losses.append(loss.item())
+    assert losses[1] < 0.1 * losses[0], losses

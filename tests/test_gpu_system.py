@@ -212,3 +212,30 @@ def test_autotune_keeps_state(cuda):
         b.update(7)
         np.testing.assert_array_equal(a.get_array(ARRAY_POS), b.get_array(ARRAY_POS))
         np.testing.assert_array_equal(a.get_array(ARRAY_VEL), b.get_array(ARRAY_VEL))
+
+
+def test_crowded_cells_keep_stable_order(cuda):
+    """Cells of every size tier (<= 32, <= 1024, <= 16384 and beyond, the
+    last sorted through global scratch) come out in (hash, original index)
+    order, as the reference's stable sort leaves them."""
+    rng = np.random.default_rng(5)
+    h = configs.H_DAMBREAK
+    # clusters inside single cells (cell = h): 20000, 3000 and 600 particles
+    def cluster(lo, n):
+        return rng.uniform([lo] * 3, [lo + 0.3 * h] * 3, (n, 3))
+    parts = [cluster(0.30, 20000), cluster(0.51, 3000), cluster(0.71, 600),
+             rng.uniform([0.15, 0.15, 0.15], [0.85, 0.85, 0.85], (6400, 3))]
+    pos = np.ones((30000, 4), np.float32)
+    pos[:, :3] = np.concatenate(parts)
+    pos = pos[rng.permutation(len(pos))]
+    vel = np.zeros_like(pos)
+    xml = configs.scene_xml(**configs.dambreak_attrs(len(pos), (0, 0, 0), (1, 1, 1)))
+    p = Scene.parse(xml).params
+    with system_from(p, pos, vel) as s:
+        s.update(1)
+        sh, cs, _ = s.cells()
+    o = oracle.full_stages(p, pos, vel)
+    cnt = np.bincount(o["sorted"][:, 0], minlength=p.numCells)
+    assert cnt.max() > 16384 and ((cnt > 1024) & (cnt <= 16384)).any() and ((cnt > 32) & (cnt <= 1024)).any()
+    np.testing.assert_array_equal(sh, o["sorted"])
+    np.testing.assert_array_equal(cs, o["cell_start"])
