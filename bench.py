@@ -59,6 +59,23 @@ def dist_env():
         int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(value: float, device=None) -> float:
+    """Largest `value` over all ranks (the job's time is its slowest rank's);
+    the value itself when no process group is initialised."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(particles_per_rank: int, steps: int, world: int, max_ms: float) -> float:
+    """Whole-job particle-steps/s: every rank steps its own replica."""
+    return world * particles_per_rank * steps / (max_ms / 1e3)
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -407,13 +424,9 @@ def main():
         torch.distributed.barrier()
     clk = clocks.stop()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms), device="cuda")
     n = sysm.n
-    value = world * n * args.steps / (total_ms / 1e3)
+    value = job_throughput(n, args.steps, world, total_ms)
 
     # warm multi-step throughput (graph replay, L2 not flushed): informative
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -465,11 +478,8 @@ def main():
         sysm.get_array(ARRAY_VEL, hvel.numpy())
     ee.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = es.elapsed_time(ee)
-    t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = world * n * args.e2e_steps / (float(t.item()) / 1e3)
+    e2e_ms = max_over_ranks(es.elapsed_time(ee), device="cuda")
+    e2e_value = job_throughput(n, args.e2e_steps, world, e2e_ms)
 
     learned = measure_learned(sysm, p, stream, args) if rank == 0 else None
 

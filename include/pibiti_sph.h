@@ -235,9 +235,11 @@ int sph_mlp_adam(float* params, float* m, float* v, const float* grad, float lr,
 /* The learned step on a system handle.  A coarse step is one whole step
    with the time step multiplied by `substeps` whose force pass also writes
    16 features per particle; the MLP then adds a velocity correction
-   y * out_scale * |g| * dt_coarse.  After every coarse step a density check
-   runs: if any scene's mean density moved by more than `tol` (relative)
-   over the step, or any value is not finite, the state is restored and the
+   dv = y * out_scale * |g| * dt_coarse, and pos_factor * dv * dt_coarse to
+   the position (default pos_factor 1/2).  After every coarse step a density
+   check runs: if any scene's mean density departs from the linear
+   extrapolation of its last two accepted steps by more than `tol` times its
+   last value, or any value is not finite, the state is restored and the
    scene set advances by `substeps` plain steps of the original time step
    instead (counted in *fallbacks). */
 /* Model: FP32 parameters (host, sph_mlp_param_count() floats), feature
@@ -246,6 +248,7 @@ int sph_learned_set_model(SphSystem* sys, const float* params, const float* feat
                           const float* out_scale);
 int sph_learned_step(SphSystem* sys, uint32_t coarse_steps, uint32_t substeps, float tol,
                      uint32_t* fallbacks);
+int sph_learned_set_options(SphSystem* sys, float pos_factor);
 /* Training data: one coarse step (no correction) that writes the raw FP32
    features (device, N x 16, sorted order) and the original index of each
    sorted slot (device, N); the state advances by that coarse step. */

@@ -198,17 +198,85 @@ void orc_force_f64(const SimParams* p, const float* sorted_pos, const float* sor
   }
 }
 
+/* FETCH of a float4 array through a texture bound to n entries: zeros
+   outside it. */
+static inline void fetch4(const float* a, uint32_t n, uint32_t j, float out[4]) {
+  const int32_t x = (int32_t)j;
+  if (x >= 0 && (uint32_t)x < n) memcpy(out, a + 4 * (size_t)x, 16);
+  else out[0] = out[1] = out[2] = out[3] = 0.f;
+}
+
+static inline float dot4(const float* a, const float* b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2] + a[3] * b[3];
+}
+
+/* The trapped-air sum of the CLR_Vel foam estimate (System.cu:429-470):
+   cells visited x outermost, then y, then z; each walk re-fetches the cell
+   start (an empty cell reads 0xFFFFFFFF, so the walk starts at index -1,
+   whose texture fetch returns zeros: for cell 0 that zero record is taken
+   as a particle at the origin at rest); float4 normalise and dot include w;
+   weight W(x, 3) = (1 - x) / 3. */
+static float foam_vdiff(const SimParams* p, const float* spos, const float* svel,
+                        const uint32_t* kv, const uint32_t* cs, uint32_t n, uint32_t index) {
+  const float* pi = spos + 4 * (size_t)index;
+  const float* vi = svel + 4 * (size_t)index;
+  int g[3];
+  grid_pos(p, pi, g);
+  float vdiff = 0.0f;
+  for (int x = -1; x < 2; ++x)
+    for (int y = -1; y < 2; ++y)
+      for (int z = -1; z < 2; ++z)
+        for (uint32_t i = 0; i < p->maxParInCell; ++i) {
+          const uint32_t gh = grid_hash(p, g[0] + x, g[1] + y, g[2] + z);
+          const uint32_t start = fetch_cell_start(cs, p->numCells, gh);
+          const uint32_t j = start + i;
+          if (fetch_key(kv, n, j) != gh) break;
+          if (j == index) continue;
+          float v2[4], x2[4], sv[4], sx[4], dv[4], dx[4];
+          fetch4(svel, n, j, v2);
+          fetch4(spos, n, j, x2);
+          for (int k = 0; k < 4; ++k) {
+            sv[k] = vi[k] + v2[k];
+            sx[k] = pi[k] + x2[k];
+            dv[k] = vi[k] - v2[k];
+            dx[k] = pi[k] - x2[k];
+          }
+          const float iv = 1.0f / sqrtf(dot4(sv, sv)), ix = 1.0f / sqrtf(dot4(sx, sx));
+          for (int k = 0; k < 4; ++k) {
+            sv[k] = sv[k] * iv;
+            sx[k] = sx[k] * ix;
+          }
+          const float r = sqrtf(dot4(dx, dx));
+          const float w = r <= 3.0f ? (1 - r) / 3.0f : 0.0f;
+          vdiff = vdiff + sqrtf(dot4(dv, dv)) * (1.0f - dot4(sv, sx)) * w;
+        }
+  return vdiff;
+}
+
+static inline float phi_clamp(float I, float tmin, float tmax) {
+  return (fminf(I, tmax) - fminf(I, tmin)) / (tmax - tmin);
+}
+
 /* Colour and dye of computeForceD (System.cu:405-546) for one particle.
-   `add` is the velocity increment the force pass produced.  CLR_Vel (the
-   foam estimate, a second neighbour walk) is not restated: the colour is
-   left untouched for it. */
+   `add` is the velocity increment the force pass produced, `vdiff` the
+   foam sum (CLR_Vel only). */
 static void color_one(const SimParams* p, const float* pos4, const float* vel4, float dens,
-                      R3_f32 add, float* dye, float* clr4) {
+                      R3_f32 add, float vdiff, float* dye, float* clr4) {
   float cx = 0.2f, cy = 0.5f, cz = 1.f, intens = 0.f;
   const float dt = p->timeStep;
   switch (p->clrType) {
     case SPH_CLR_NONE:
       return;
+    case SPH_CLR_VEL: {
+      const float v = 2.5f * len3_f32(r3_f32(vel4[0], vel4[1], vel4[2]));
+      const float clrV = p->brightness + p->contrast * v;
+      intens = clrV;
+      const float trapped = phi_clamp(vdiff, 5.0f, 20.0f);
+      const float kEnergy = (float)((double)(p->particleMass * 1000 * dot4(vel4, vel4)) * 0.5);
+      const float kPot = phi_clamp(kEnergy, 0.1f, 1.0f);
+      const float Nd = kPot * (3.0f * trapped + 3.0f * 0.0f);
+      cx = cy = cz = Nd;
+    } break;
     case SPH_CLR_VELACC: {
       const float v = 2.5f * len3_f32(r3_f32(vel4[0], vel4[1], vel4[2]));
       const float f = 0.02f * len3_f32(add) / dt;
@@ -294,9 +362,13 @@ void orc_force_color_f32(const SimParams* p, const float* sorted_pos, const floa
     R3_f32 add;
     force_one_f32(p, sorted_pos, sorted_vel, density, pressure, kv, cell_start, n, (uint32_t)i,
                   new_vel + 4 * (size_t)si, &add, 0);
-    if (clr && dye)
-      color_one(p, sorted_pos + 4 * i, sorted_vel + 4 * i, density[i], add, dye + si,
+    if (clr && dye) {
+      const float vdiff = p->clrType == SPH_CLR_VEL
+                              ? foam_vdiff(p, sorted_pos, sorted_vel, kv, cell_start, n, (uint32_t)i)
+                              : 0.f;
+      color_one(p, sorted_pos + 4 * i, sorted_vel + 4 * i, density[i], add, vdiff, dye + si,
                 clr + 4 * (size_t)si);
+    }
   }
 }
 

@@ -61,8 +61,8 @@ void orc_force_f64(const SimParams* p, const float* sorted_pos, const float* sor
                    const uint32_t* cell_start, uint32_t n, double* new_vel, double* scale);
 
 /* The whole computeForceD in single precision: orc_force_f32 plus the
-   colour and dye outputs (System.cu:405-546), both in original order.
-   CLR_Vel (the foam estimate, a second neighbour walk) is not restated. */
+   colour and dye outputs (System.cu:405-546, including the CLR_Vel foam
+   estimate and its second neighbour walk), both in original order. */
 void orc_force_color_f32(const SimParams* p, const float* sorted_pos, const float* sorted_vel,
                          const float* density, const float* pressure, const uint32_t* kv,
                          const uint32_t* cell_start, uint32_t n, float* new_vel, float* dye,

@@ -305,12 +305,156 @@ __device__ __forceinline__ float3 collide_sphere(const SimParams& p, float3 rel,
   return f;
 }
 
+// collideSpheresR (Kernel_Cell.cui:101-115): spring and damping only.
+__device__ __forceinline__ float3 collide_sphere_r(const SimParams& p, float3 rel, float3 rv,
+                                                   float radius) {
+  const float dist = len3(rel);
+  float3 f = f3(0.f, 0.f, 0.f);
+  if (dist < radius) {
+    const float inv = __fdiv_rn(1.0f, dist);
+    const float3 n = f3(__fmul_rn(rel.x, inv), __fmul_rn(rel.y, inv), __fmul_rn(rel.z, inv));
+    const float sp = __fmul_rn(p.spring, __fsub_rn(dist, radius));
+    f.x = __fadd_rn(__fmul_rn(sp, n.x), __fmul_rn(p.damping, rv.x));
+    f.y = __fadd_rn(__fmul_rn(sp, n.y), __fmul_rn(p.damping, rv.y));
+    f.z = __fadd_rn(__fmul_rn(sp, n.z), __fmul_rn(p.damping, rv.z));
+  }
+  return f;
+}
+
+__device__ __forceinline__ void add3(float3& a, float3 b) {
+  a.x = __fadd_rn(a.x, b.x);
+  a.y = __fadd_rn(a.y, b.y);
+  a.z = __fadd_rn(a.z, b.z);
+}
+
+// Height-map collider (System.cu:253-309): collision spheres on a sine
+// surface over the XZ plane (iHmap == 1) or the YZ plane, 5 x 5 x 2 around
+// the particle.
+__device__ inline void heightmap(const SimParams& p, float4 xi, float4 vi, float3& add) {
+  const float PI_ = 3.141592654f;
+  const float3 vel3 = f3(-vi.x, -vi.y, -vi.z);
+  const float rr = __fadd_rn(p.particleR, p.rotR), spc = p.rotSpc;
+  const float o2 = __fdiv_rn(__fmul_rn(p.s2, PI_), 180.f), o4 = __fdiv_rn(__fmul_rn(p.s4, PI_), 180.f);
+  const bool xz = p.iHmap == 1;
+  // (u, z) plane coordinates: u is x for the XZ map, y for the YZ map
+  const float pu = xz ? xi.x : xi.y, umin = xz ? p.worldMin.x : p.worldMin.y;
+  const float usz = xz ? p.worldSizeD.x : p.worldSizeD.y;
+  const float hmin = xz ? p.worldMin.y : p.worldMin.x;
+  const int iu = __float2int_rz(__fdiv_rn(__fsub_rn(pu, umin), spc));
+  const float uf = __fadd_rn(__fmul_rn((float)iu, spc), umin);
+  const int iz = __float2int_rz(__fdiv_rn(__fsub_rn(xi.z, p.worldMin.z), spc));
+  const float zf = __fadd_rn(__fmul_rn((float)iz, spc), p.worldMin.z);
+#pragma unroll 1
+  for (int j = -2; j <= 2; ++j)
+#pragma unroll 1
+    for (int i = -2; i <= 2; ++i) {
+      const float uh = __fadd_rn(uf, __fmul_rn((float)i, spc));
+      const float zh = __fadd_rn(zf, __fmul_rn((float)j, spc));
+      for (int k = 0; k <= 1; ++k) {
+        const float un = __fmul_rn(__fmul_rn(__fdiv_rn(uh, usz), 2.f), PI_);
+        const float zn = __fmul_rn(__fmul_rn(__fdiv_rn(zh, p.worldSizeD.z), 2.f), PI_);
+        const float ss = __fmul_rn(sinf(__fadd_rn(__fmul_rn(p.s1, un), o2)),
+                                   sinf(__fadd_rn(__fmul_rn(p.s3, zn), o4)));
+        if (p.s5 <= -1.f || ss > p.s5) {
+          const float hf = __fadd_rn(__fadd_rn(__fmul_rn(ss, p.hClose), p.r2Angle), hmin);
+          const float hh = __fsub_rn(hf, __fmul_rn((float)k, spc));
+          const float3 rel = xz ? f3(__fsub_rn(uh, xi.x), __fsub_rn(hh, xi.y), __fsub_rn(zh, xi.z))
+                                : f3(__fsub_rn(hh, xi.x), __fsub_rn(uh, xi.y), __fsub_rn(zh, xi.z));
+          add3(add, collide_sphere_r(p, rel, vel3, rr));
+        }
+      }
+    }
+}
+
+// Rotor and propeller colliders (System.cu:311-372): rotType 1 (pump rotor
+// about z), 2 (pump rotor about y), 3 (propeller about z, optionally two).
+__device__ inline void rotor(const SimParams& p, float4 xi, float4 vi, float3& add) {
+  const float PI_ = 3.141592654f;
+  const int sx = p.rotSize.x, sy = p.rotSize.y, sz = p.rotSize.z, cb = p.rotBlades;
+  const float sp = p.rotSpc, ca = __fdiv_rn(__fmul_rn(2.f, PI_), (float)cb);
+  const float x2 = __fmul_rn((float)sx, 0.5f), y2 = __fmul_rn((float)sy, 0.5f);
+  const float rr = __fadd_rn(p.particleR, p.rotR);
+  const float3 vel3 = f3(-vi.x, -vi.y, -vi.z);
+  const float cx = p.collPos.x, cy = p.collPos.y, cz = p.collPos.z;
+  if (p.rotType == 1 || p.rotType == 2) {
+    const bool zrot = p.rotType == 1;
+    const float pa = zrot ? xi.z : xi.y, ca0 = zrot ? cz : cy;
+    if (!(pa > __fsub_rn(ca0, rr) && pa < __fadd_rn(__fadd_rn(ca0, rr), __fmul_rn(sp, (float)sy))))
+      return;
+#pragma unroll 1
+    for (int z = 1; z <= sz; ++z)
+#pragma unroll 1
+      for (int x = 0; x <= sx; ++x)
+#pragma unroll 1
+        for (int c = 0; c < cb; ++c) {
+          const float a = __fadd_rn(__fadd_rn(-p.rAngle, __fmul_rn((float)c, ca)),
+                                    __fmul_rn((float)z, p.rTwist));
+          const float cs = __fmul_rn(cosf(a), sp), sn = __fmul_rn(-sinf(a), sp);
+          const float xx = __fsub_rn((float)x, x2);
+          const float q0 = __fsub_rn(__fmul_rn(xx, cs), __fmul_rn((float)z, sn));
+          const float q1 = __fadd_rn(__fmul_rn(xx, sn), __fmul_rn((float)z, cs));
+#pragma unroll 1
+          for (int y = 0; y <= sy; ++y) {
+            const float qy = __fmul_rn(sp, (float)y);
+            const float3 rel =
+                zrot ? f3(__fsub_rn(__fadd_rn(cx, q0), xi.x), __fsub_rn(__fadd_rn(cy, q1), xi.y),
+                          __fsub_rn(__fadd_rn(cz, qy), xi.z))
+                     : f3(__fsub_rn(__fadd_rn(cx, q0), xi.x), __fsub_rn(__fadd_rn(cy, qy), xi.y),
+                          __fsub_rn(__fadd_rn(cz, q1), xi.z));
+            add3(add, collide_sphere_r(p, rel, vel3, rr));
+          }
+        }
+  } else if (p.rotType == 3) {
+    const float half = __fdiv_rn(__fmul_rn(sp, (float)sz), 2.f);
+    if (!(xi.z > __fsub_rn(__fsub_rn(cz, rr), half) && xi.z < __fadd_rn(__fadd_rn(cz, rr), half))) return;
+    float rx = cx, aa = p.rAngle, tw = p.rTwist;
+    if (p.r2Dist > 0.f) {
+      if (xi.x > 0.f) {
+        rx = __fadd_rn(rx, __fmul_rn(p.r2Dist, 0.5f));
+      } else {
+        rx = __fsub_rn(rx, __fmul_rn(p.r2Dist, 0.5f));
+        aa = p.r2Angle;
+        tw = __fmul_rn(tw, p.r2twist);
+      }
+    }
+#pragma unroll 1
+    for (int c = 0; c < cb; ++c) {
+      const float a = __fadd_rn(aa, __fmul_rn((float)c, ca));
+#pragma unroll 1
+      for (int h = 0; h <= sy; ++h) {
+        float dh = 0.f;
+        if (h == sy - 1) dh = 0.5f;
+        else if (h == sy) dh = 1.2f;
+#pragma unroll 1
+        for (int x = 0; x <= sz; ++x) {
+          float d = dh;
+          if (x == sz && d == 0.f) d = 0.4f;
+          const float k = cosf(__fadd_rn(__fmul_rn(__fsub_rn((float)x, x2), 0.2f), __fmul_rn(PI_, 0.6f)));
+          const float at = __fmul_rn(tw, __fsub_rn(__fmul_rn(d, -0.05f), __fmul_rn(__fsub_rn((float)h, y2), k)));
+          const float ac = __fadd_rn(a, at);
+          const float cs = __fmul_rn(cosf(ac), sp), sn = __fmul_rn(-sinf(ac), sp);
+          const float qx = __fmul_rn((float)x, cs), qy = __fmul_rn((float)x, sn);
+          const float qz = __fmul_rn(__fmul_rn(sp, __fsub_rn(__fadd_rn(-d, (float)h), y2)), k);
+          const float r = __fmul_rn(p.rotR, fabsf(__fsub_rn(1.f, d)));
+          const float3 rel = f3(__fsub_rn(__fadd_rn(rx, qx), xi.x), __fsub_rn(__fadd_rn(cy, qy), xi.y),
+                                __fsub_rn(__fadd_rn(cz, qz), xi.z));
+          add3(add, collide_sphere_r(p, rel, vel3, __fadd_rn(p.particleR, r)));
+        }
+      }
+    }
+  }
+}
+
 // The part of computeForceD after the neighbour sums (System.cu:249-250,
-// 373-402): dv = F m dt, plus the sphere collider and the accelerators.
+// 253-402): dv = F m dt, the height map, the rotor or the sphere collider,
+// and the accelerators.
 __device__ inline float3 velocity_increment(const SimParams& p, float3 F, float4 xi, float4 vi) {
   const float s = __fmul_rn(p.particleMass, p.timeStep);
   float3 add = f3(__fmul_rn(F.x, s), __fmul_rn(F.y, s), __fmul_rn(F.z, s));
-  if (p.rotType <= 0) {
+  if (p.iHmap > 0) heightmap(p, xi, vi, add);
+  if (p.rotType > 0) {
+    rotor(p, xi, vi, add);
+  } else {
     const float3 rel = f3(__fsub_rn(p.collPos.x, xi.x), __fsub_rn(p.collPos.y, xi.y),
                           __fsub_rn(p.collPos.z, xi.z));
     const float3 c = collide_sphere(p, rel, f3(-vi.x, -vi.y, -vi.z), __fadd_rn(p.particleR, p.collR));
@@ -350,13 +494,48 @@ __device__ inline float3 velocity_increment(const SimParams& p, float3 F, float4
   return add;
 }
 
-// Colour and dye of computeForceD (System.cu:405-546).  Returns false when
-// nothing is written (CLR_None, or CLR_Vel whose foam estimate is not built).
+__device__ __forceinline__ float dot4(float4 a, float4 b) {
+  return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z)),
+                   __fmul_rn(a.w, b.w));
+}
+
+// One term of the CLR_Vel trapped-air sum (System.cu:453-460): relative
+// speed x (1 - cos between the normalised (4-component) velocity and position
+// sums) x W(distance, 3) with W(x, h) = (1 - x)/h for x <= h.
+__device__ __forceinline__ float foam_term(float4 xi, float4 vi, float4 xj, float4 vj) {
+  float4 sv = make_float4(__fadd_rn(vi.x, vj.x), __fadd_rn(vi.y, vj.y), __fadd_rn(vi.z, vj.z), __fadd_rn(vi.w, vj.w));
+  float4 sx = make_float4(__fadd_rn(xi.x, xj.x), __fadd_rn(xi.y, xj.y), __fadd_rn(xi.z, xj.z), __fadd_rn(xi.w, xj.w));
+  const float4 dv = make_float4(__fsub_rn(vi.x, vj.x), __fsub_rn(vi.y, vj.y), __fsub_rn(vi.z, vj.z), __fsub_rn(vi.w, vj.w));
+  const float4 dx = make_float4(__fsub_rn(xi.x, xj.x), __fsub_rn(xi.y, xj.y), __fsub_rn(xi.z, xj.z), __fsub_rn(xi.w, xj.w));
+  const float iv = __fdiv_rn(1.0f, __fsqrt_rn(dot4(sv, sv))), ix = __fdiv_rn(1.0f, __fsqrt_rn(dot4(sx, sx)));
+  sv = make_float4(__fmul_rn(sv.x, iv), __fmul_rn(sv.y, iv), __fmul_rn(sv.z, iv), __fmul_rn(sv.w, iv));
+  sx = make_float4(__fmul_rn(sx.x, ix), __fmul_rn(sx.y, ix), __fmul_rn(sx.z, ix), __fmul_rn(sx.w, ix));
+  const float r = __fsqrt_rn(dot4(dx, dx));
+  const float w = r <= 3.0f ? __fdiv_rn(__fsub_rn(1.f, r), 3.0f) : 0.0f;
+  return __fmul_rn(__fmul_rn(__fsqrt_rn(dot4(dv, dv)), __fsub_rn(1.0f, dot4(sv, sx))), w);
+}
+
+__device__ __forceinline__ float phi_clamp(float I, float tmin, float tmax) {
+  return __fdiv_rn(__fsub_rn(fminf(I, tmax), fminf(I, tmin)), __fsub_rn(tmax, tmin));
+}
+
+// Colour and dye of computeForceD (System.cu:405-546); `vdiff` is the
+// foam sum for CLR_Vel.  Returns false when nothing is written (CLR_None).
 __device__ inline bool color_dye(const SimParams& p, float4 xi, float4 vi, float dens, float3 add,
-                                 float* dye, float4& clr) {
+                                 float vdiff, float* dye, float4& clr) {
   float cx = 0.2f, cy = 0.5f, cz = 1.f, intens = 0.f;
   const float dt = p.timeStep;
   switch (p.clrType) {
+    case SPH_CLR_VEL: {
+      const float v = __fmul_rn(2.5f, len3(f3(vi.x, vi.y, vi.z)));
+      const float clrV = __fadd_rn(p.brightness, __fmul_rn(p.contrast, v));
+      intens = clrV;
+      const float trapped = phi_clamp(vdiff, 5.0f, 20.0f);
+      const float kEnergy = __fmul_rn(__fmul_rn(__fmul_rn(p.particleMass, 1000.f), dot4(vi, vi)), 0.5f);
+      const float kPot = phi_clamp(kEnergy, 0.1f, 1.0f);
+      const float Nd = __fmul_rn(kPot, __fadd_rn(__fmul_rn(3.0f, trapped), __fmul_rn(3.0f, 0.0f)));
+      cx = cy = cz = Nd;
+    } break;
     case SPH_CLR_VELACC: {
       const float v = __fmul_rn(2.5f, len3(f3(vi.x, vi.y, vi.z)));
       const float f = __fdiv_rn(__fmul_rn(0.02f, len3(add)), dt);

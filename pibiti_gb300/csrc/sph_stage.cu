@@ -55,8 +55,10 @@ int validate_params(const SimParams& p, bool fused) {
     return fail(SPH_ERR_PARAMS, "cellSize must be positive");
   if (!(p.h > 0.f) || !(p.timeStep == p.timeStep))
     return fail(SPH_ERR_PARAMS, "h must be positive and timeStep finite");
-  if (p.iHmap > 0) return fail(SPH_ERR_UNSUPPORTED, "height-map collider (iHmap > 0) is not implemented");
-  if (p.rotType > 0) return fail(SPH_ERR_UNSUPPORTED, "rotor/propeller collider (rotType > 0) is not implemented");
+  if (p.rotType > 3) return fail(SPH_ERR_PARAMS, "unknown rotType %d", p.rotType);
+  if (p.rotType > 0 && p.rotBlades <= 0) return fail(SPH_ERR_PARAMS, "rotor needs rotBlades > 0");
+  if ((p.iHmap > 0 || p.rotType > 0) && !(p.rotSpc > 0.f))
+    return fail(SPH_ERR_PARAMS, "height map and rotor need rotSpc > 0");
   if (p.bndType > SPH_BND_PUMP_Y) return fail(SPH_ERR_PARAMS, "unknown bndType %u", p.bndType);
   if (fused) {
     // The fused kernels skip neighbour cells outside the grid.  The
@@ -159,8 +161,8 @@ __global__ void st_density(const SimParams p, const float4* __restrict__ spos,
   density[i] = dens;
 }
 
-// computeForceD (System.cu:228-250, 373-546 without rotor, height map and
-// foam): new velocity, colour and dye in original order through hash[i].y.
+// computeForceD (System.cu:228-546): new velocity, colour (with the foam
+// estimate) and dye in original order through hash[i].y.
 __global__ void st_force(const SimParams p, const float4* __restrict__ spos,
                          const float4* __restrict__ svel, const float* __restrict__ pressure,
                          const float* __restrict__ density, const uint2* __restrict__ hash,
@@ -196,8 +198,25 @@ __global__ void st_force(const SimParams p, const float4* __restrict__ spos,
   new_vel[si] = make_float4(__fadd_rn(vi.x, add.x), __fadd_rn(vi.y, add.y), __fadd_rn(vi.z, add.z),
                             __fadd_rn(vi.w, 0.f));
   if (clr) {
+    float vdiff = 0.f;
+    if (p.clrType == SPH_CLR_VEL) {
+      // the foam walk (System.cu:441-468): x outermost, the cell start
+      // re-read per entry, an empty cell starting at index -1 (a zero record)
+      for (int x = -1; x < 2; ++x)
+        for (int y = -1; y < 2; ++y)
+          for (int z = -1; z < 2; ++z)
+            for (uint32_t q = 0; q < p.maxParInCell; ++q) {
+              const uint32_t gh = grid_hash_raw(p, g.x + x, g.y + y, g.z + z);
+              const uint32_t j = ref_cell_start(cs, num_cells, gh) + q;
+              if (ref_key(hash, n, j) != gh) break;
+              if (j == i) continue;
+              const bool in = (int)j >= 0 && j < n;
+              const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+              vdiff = __fadd_rn(vdiff, foam_term(xi, vi, in ? spos[j] : zero, in ? svel[j] : zero));
+            }
+    }
     float4 c;
-    if (color_dye(p, xi, vi, di, add, dye ? dye + si : nullptr, c)) clr[si] = c;
+    if (color_dye(p, xi, vi, di, add, vdiff, dye ? dye + si : nullptr, c)) clr[si] = c;
   }
 }
 
@@ -311,8 +330,6 @@ int sph_collide(const sph_float4* oldPos, sph_float4* newPos, sph_float4* clr,
   (void)newPos;
   (void)oldVel;
   SPH_TRY(need_params());
-  if (clr && g_params.clrType == SPH_CLR_VEL)
-    return fail(SPH_ERR_UNSUPPORTED, "collide: colour type CLR_Vel (foam estimate) is not implemented");
   if (numParticles == 0) return SPH_OK;
   const unsigned grid = grid_for(numParticles, 64);
   st_density<<<grid, 64, 0, g_stage_stream>>>(g_params, (const float4*)sortedPos,

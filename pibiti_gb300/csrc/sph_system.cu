@@ -491,21 +491,34 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   }
 }
 
-// vel[i] += y[i] * out_scale * g * dt (the MLP's correction, sorted order).
+// The MLP's correction, sorted order: dv = y * out_scale * g * dt added to
+// the velocity and pos_factor * dv * dt to the position (pos_factor = 1/2
+// is the position change of a constant extra acceleration over the step).
 __global__ void k_apply_correction(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff,
                                    int S, uint32_t N, const float* __restrict__ y,
-                                   const float* __restrict__ out_scale, float4* __restrict__ vel) {
+                                   const float* __restrict__ out_scale, float pos_factor,
+                                   float4* __restrict__ pos, float4* __restrict__ vel) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const SimParams& p = sc[S == 1 ? 0 : scene_of(poff, S, i)].p;
   const float g = sqrtf(p.gravity.x * p.gravity.x + p.gravity.y * p.gravity.y +
                         p.gravity.z * p.gravity.z) + 1e-6f;
   const float u = g * p.timeStep;
+  const float dvx = y[3 * i + 0] * out_scale[0] * u, dvy = y[3 * i + 1] * out_scale[1] * u,
+              dvz = y[3 * i + 2] * out_scale[2] * u;
   float4 v = vel[i];
-  v.x += y[3 * i + 0] * out_scale[0] * u;
-  v.y += y[3 * i + 1] * out_scale[1] * u;
-  v.z += y[3 * i + 2] * out_scale[2] * u;
+  v.x += dvx;
+  v.y += dvy;
+  v.z += dvz;
   vel[i] = v;
+  if (pos_factor != 0.f) {
+    const float k = pos_factor * p.timeStep;
+    float4 x = pos[i];
+    x.x += dvx * k;
+    x.y += dvy * k;
+    x.z += dvz * k;
+    pos[i] = x;
+  }
 }
 
 // ---- buffer API kernels ---------------------------------------------------
@@ -630,6 +643,7 @@ struct SphSystem {
   void* mlp_img = nullptr;           // packed BF16 weights
   float* mlp_aux = nullptr;          // feature mean[16], inv_std[16], out_scale[3]
   bool model_set = false;
+  float pos_factor = 0.5f;           // position part of the correction
   uint16_t* feat = nullptr;          // N x 16 standardised features (BF16)
   float* mlp_y = nullptr;            // N x 3 corrections
   float4* bk_pos = nullptr;          // checkpoint for the fallback
@@ -1116,6 +1130,12 @@ int sph_learned_set_model(SphSystem* s, const float* params, const float* feat_s
   return rc;
 }
 
+int sph_learned_set_options(SphSystem* s, float pos_factor) {
+  if (!s || !(pos_factor == pos_factor)) return fail(SPH_ERR_ARG, "learned_set_options: bad arguments");
+  s->pos_factor = pos_factor;
+  return SPH_OK;
+}
+
 int sph_features_step(SphSystem* s, uint32_t substeps, float* feat_raw, uint32_t* ids) {
   if (!s || substeps == 0) return fail(SPH_ERR_ARG, "features_step: bad arguments");
   if (s->coarse_sub != substeps) SPH_TRY(ensure_coarse(s, substeps));
@@ -1140,8 +1160,8 @@ int sph_learned_step(SphSystem* s, uint32_t coarse_steps, uint32_t substeps, flo
   if (!s->bk_pos) SPH_TRY(dalloc(&s->bk_pos, s->N, "checkpoint"));
   if (!s->bk_vel) SPH_TRY(dalloc(&s->bk_vel, s->N, "checkpoint"));
   if (!s->bk_id) SPH_TRY(dalloc(&s->bk_id, s->N, "checkpoint"));
-  std::vector<double> st, ref;
-  bool have_ref = false;
+  std::vector<double> st, ref, ref2;
+  bool have_ref = false, have_ref2 = false;
   if (s->stepped) {
     SPH_TRY(scene_stats(s, ref));
     have_ref = true;
@@ -1159,17 +1179,20 @@ int sph_learned_step(SphSystem* s, uint32_t coarse_steps, uint32_t substeps, flo
     SPH_TRY(enqueue_step(s, s->stream, nullptr, &o));
     SPH_TRY(sph_mlp_forward(s->mlp_img, s->feat, s->N, s->mlp_y, s->stream));
     k_apply_correction<<<grid_for(s->N, kBlock), kBlock, 0, s->stream>>>(
-        s->d_coarse, s->d_poff, s->S, s->N, s->mlp_y, s->mlp_aux + 32, s->vel[s->cv]);
+        s->d_coarse, s->d_poff, s->S, s->N, s->mlp_y, s->mlp_aux + 32, s->pos_factor,
+        s->pos[s->cp], s->vel[s->cv]);
     SPH_CUDA(cudaGetLastError(), "apply correction");
-    // density-deviation check: every scene's mean density may move by at
-    // most `tol` (relative) over the coarse step, and nothing may be NaN/Inf
+    // density-deviation check, per scene: the mean density of the step may
+    // depart from the linear extrapolation of the last two accepted steps
+    // by at most tol (relative), and nothing may be NaN/Inf
     SPH_TRY(scene_stats(s, st));
     bool ok = true;
     for (int i = 0; i < s->S && ok; ++i) {
       if (st[4 * i + 3] != 0.0 || !(st[4 * i + 1] == st[4 * i + 1])) ok = false;
       if (have_ref && ok) {
-        const double r0 = ref[4 * i + 1];
-        if (!(fabs(st[4 * i + 1] - r0) <= tol * r0)) ok = false;
+        const double r1 = ref[4 * i + 1];
+        const double pred = have_ref2 ? 2.0 * r1 - ref2[4 * i + 1] : r1;
+        if (!(fabs(st[4 * i + 1] - pred) <= tol * r1)) ok = false;
       }
     }
     if (!ok) {  // fall back: restore and take `substeps` fine steps
@@ -1182,6 +1205,8 @@ int sph_learned_step(SphSystem* s, uint32_t coarse_steps, uint32_t substeps, flo
       for (uint32_t q = 0; q < substeps; ++q) SPH_TRY(enqueue_step(s, s->stream));
       SPH_TRY(scene_stats(s, st));
     }
+    ref2 = ref;
+    have_ref2 = have_ref;
     ref = st;
     have_ref = true;
   }

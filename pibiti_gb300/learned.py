@@ -71,6 +71,11 @@ def learned_step(sph: SPH, coarse_steps: int, substeps: int = SUBSTEPS, tol: flo
     return fb.value
 
 
+def set_options(sph: SPH, pos_factor: float = 0.5) -> None:
+    """Position part of the correction (pos_factor * dv * dt_coarse)."""
+    _lib.check(_lib.lib().sph_learned_set_options(sph._h, pos_factor))
+
+
 def features_step(sph: SPH, feat, ids, substeps: int = SUBSTEPS) -> None:
     _lib.check(_lib.lib().sph_features_step(sph._h, substeps, _p(feat), _p(ids)))
 
@@ -200,7 +205,7 @@ def one_step_errors(model: Model, xml: str, pos, vel, warm: int = 40,
 
 
 def rollout(model: Model, xml: str, pos, vel, fine_steps: int, substeps: int = SUBSTEPS,
-            tol: float = 0.01, warm: int = 0) -> dict:
+            tol: float = 0.01, warm: int = 0, pos_factor: float = 0.5) -> dict:
     """Mean-density trajectories of the fine-dt plain run, the coarse run
     without the network and the learned run, sampled every `substeps` fine
     steps; errors relative to the fine run, and the wall time of each."""
@@ -234,6 +239,7 @@ def rollout(model: Model, xml: str, pos, vel, fine_steps: int, substeps: int = S
         lrn.set_array(ARRAY_POS, s_pos)
         lrn.set_array(ARRAY_VEL, s_vel)
         model.install(lrn)
+        set_options(lrn, pos_factor)
         rho_l, fb = [], 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()

@@ -132,6 +132,13 @@ def make_steps():
     posc, velc = oracle.step(pc, posc, velc, steps=20)
     save_step("features", pc, posc, velc, "default scene, collider, accelerators, colour, dye")
 
+    # C2: the same state with the CLR_Vel colour (the foam estimate and its
+    #     second neighbour walk, System.cu:425-498); clrType is not an XML
+    #     attribute, so it is set on the parameters
+    pf = pc.copy()
+    pf.clrType = 3
+    save_step("foam", pf, posc, velc, "CLR_Vel foam colour with dye")
+
     # D: a grid of more than 65536 cells: 32-bit sort passes
     wd = configs.dambreak_small(side=8)
     xmld = configs.scene_xml(**configs.dambreak_attrs(1024, (0.0, 0.0, 0.0), (2.2, 2.0, 2.2)))
@@ -144,6 +151,28 @@ def make_steps():
     assert pd.numCells >= 65536, pd.numCells
     save_step("bigrid", pd, posd, veld, f"{pd.numCells} cells, 32-bit sort")
     del wd
+
+    # F-I: the rotor/propeller and height-map colliders (System.cu:253-372)
+    rng = np.random.default_rng(21)
+    for name, attrs in (("rotor", 'RotorType="1" RotorAngle="20" RotorTwist="0.3"'),
+                        ("propeller", 'RotorType="3" RotorSizes="0 3 8" Rotor2Dist="0.12" '
+                                      'Rotor2Angle="40" RotorBlades="3"'),
+                        ("hmapxz", 'HmapType="1" Hheight="0.02" Hscale="0.05" HxFq="2" HzFq="3" '
+                                   'HholeR="-2"'),
+                        ("hmapyz", 'HmapType="2" Hheight="0.02" Hscale="0.05" HxFq="2" HzFq="3" '
+                                   'HholeR="0.2"')):
+        pr, _ = ref_scene_from_xml(f'<Scene Particles="2048" {attrs} />')
+        wmin = np.array([pr.worldMin.x, pr.worldMin.y, pr.worldMin.z])
+        wmax = np.array([pr.worldMax.x, pr.worldMax.y, pr.worldMax.z])
+        pos = np.ones((2048, 4), np.float32)
+        if name in ("rotor", "propeller"):  # around the rotor axis position
+            c = np.array([pr.collPos.x, pr.collPos.y, pr.collPos.z])
+            pos[:, :3] = np.clip(c + rng.normal(0, 0.03, size=(2048, 3)), wmin + 0.01, wmax - 0.01)
+        else:
+            pos[:, :3] = rng.uniform(wmin + 0.01, wmax - 0.01, size=(2048, 3))
+        vel = np.zeros((2048, 4), np.float32)
+        vel[:, :3] = rng.normal(0, 0.2, size=(2048, 3))
+        save_step(name, pr, pos, vel, f"collider: {attrs}")
 
     # E: fewer particles than one block
     w = configs.dambreak_small(side=4)

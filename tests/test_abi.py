@@ -68,10 +68,10 @@ def test_errors_are_status_codes():
 def test_invalid_params_rejected():
     from pibiti_gb300.sph import Scene
     p = Scene.default().params
-    p.iHmap = 1
+    p.rotType = 7
     with pytest.raises(_lib.SphError) as e:
         _lib.check(_lib.lib().sph_setParameters(ctypes.byref(p)))
-    assert e.value.code == 4
+    assert e.value.code == 3
     p = Scene.default().params
     p.numCells += 1
     with pytest.raises(_lib.SphError) as e:

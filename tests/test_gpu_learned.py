@@ -51,13 +51,24 @@ def test_fallback_reproduces_fine_steps(cuda):
         np.testing.assert_array_equal(a.get_array(ARRAY_VEL), b.get_array(ARRAY_VEL))
 
 
+def test_training_lowers_loss(cuda):
+    """The project's own forward/backward kernels and Adam, run on a small
+    ensemble, lower the training loss."""
+    e = configs.ensemble(scenes=8, nmin=4096, nmax=8192, seed=3)
+    f, t = learned.generate(e.xmls, e.pos, e.vel, e.sizes, snapshots=4)
+    model = learned.train(f, t, epochs=4, batch=16384)
+    h = model.info["loss_history"]
+    assert np.isfinite(model.params).all()
+    assert h[-1] < 0.9 * h[0], h
+
+
 def test_trained_network_gains(cuda):
-    """A network trained on a small ensemble reduces the one-step velocity
-    error of the 4x dt step against four dt steps on a dam break it has not
-    seen, compared with the 4x dt step without it."""
-    e = configs.ensemble(scenes=12, nmin=4096, nmax=8192, seed=3)
-    f, t = learned.generate(e.xmls, e.pos, e.vel, e.sizes, snapshots=6)
-    model = learned.train(f, t, epochs=6, batch=16384)
-    w = configs.dambreak_small(side=16, seed=9)
-    err = learned.one_step_errors(model, w.xml, w.pos, w.vel)
-    assert err["coarse_learned"] < 0.8 * err["coarse_plain"], err
+    """The shipped network (trained on the 256-scene ensemble with the
+    project's kernels) reduces the one-step velocity error of the 4x dt step
+    against four dt steps, on dam breaks it has not seen, compared with the
+    4x dt step without it."""
+    model = learned.Model.load()
+    for side, seed in ((16, 9), (24, 11)):
+        w = configs.dambreak_small(side=side, seed=seed)
+        err = learned.one_step_errors(model, w.xml, w.pos, w.vel)
+        assert err["coarse_learned"] < 0.85 * err["coarse_plain"], (side, err)

@@ -5,7 +5,8 @@ and against the oracle.
 Bit-exact: integrate, calcHash, RadixSort, reorder.  Density: within
 DENS_RTOL of the double-precision oracle; new velocity: the difference to
 the double-precision oracle within VEL_RTOL times the sum of the magnitudes
-of the increments that were added (plus 4 ulp of the velocity itself).
+of the increments that were added (plus 4 ulp of the velocity itself, and
+for the height-map and rotor colliders a conditioning term, check_force).
 """
 import numpy as np
 import pytest
@@ -17,7 +18,8 @@ pytestmark = pytest.mark.gpu
 
 DENS_RTOL = 1e-5
 VEL_RTOL = 1e-5
-CASES = ["dambreak", "truncate", "features", "bigrid", "tiny"]
+CASES = ["dambreak", "truncate", "features", "foam", "bigrid", "tiny", "rotor", "propeller",
+         "hmapxz", "hmapyz"]
 
 
 def dev(torch, a):
@@ -34,12 +36,43 @@ def host(t, dtype=None):
     return a
 
 
+COND_ULPS = 4
+
+
+def _conditioning(p, g_sorted, spos, svel, dens, pres, cs, v64, idx):
+    """Largest change of the FP64 new velocity of particles `idx` (original
+    indices) when their positions move by one ulp along any axis.  The
+    height-map and rotor colliders are steep or discontinuous in position
+    (sample windows, contact tests), so an FP32 evaluation is defined only to
+    within a few of these."""
+    rank = np.empty(len(g_sorted), np.int64)
+    rank[g_sorted[:, 1]] = np.arange(len(g_sorted))
+    k = rank[idx]
+    sens = np.zeros(len(idx))
+    for ax in range(3):
+        for to in (np.float32(np.inf), np.float32(-np.inf)):
+            sp = spos.copy()
+            sp[k, ax] = np.nextafter(sp[k, ax], to)
+            v2, _ = oracle.force(p, sp, svel, dens, pres, g_sorted, cs, fp64=True)
+            sens = np.maximum(sens, np.abs(v2[idx, :3] - v64[idx, :3]).max(axis=1))
+    return sens
+
+
 def check_force(p, g_sorted, spos, svel, dens, pres, cs, vel_gpu):
+    """New velocities within VEL_RTOL of the FP64 oracle, relative to the sum
+    of the magnitudes of the increments; with the height-map or rotor
+    collider, plus COND_ULPS times the velocity change that a one-ulp move of
+    the particle's position causes (computed for the particles that need it)."""
     v64, scale = oracle.force(p, spos, svel, dens, pres, g_sorted, cs, fp64=True)
     vin = np.empty((len(spos), 4))
     vin[g_sorted[:, 1]] = svel
     err = np.abs(vel_gpu[:, :3].astype(np.float64) - v64[:, :3]).max(axis=1)
     bound = VEL_RTOL * scale + 4 * np.finfo(np.float32).eps * np.abs(vin[:, :3]).max(axis=1) + 1e-12
+    if p.iHmap > 0 or p.rotType > 0:
+        idx = np.nonzero(err > bound)[0]
+        assert len(idx) <= max(8, len(err) // 200), f"{len(idx)} particles outside the plain bound"
+        if len(idx):
+            bound[idx] += COND_ULPS * _conditioning(p, g_sorted, spos, svel, dens, pres, cs, v64, idx)
     assert np.all(err <= bound), f"worst err/bound {float((err / bound).max()):.3g}"
     np.testing.assert_array_equal(vel_gpu[:, 3], vin[:, 3])
 
@@ -96,7 +129,7 @@ def test_stages_vs_reference(cuda, golden, case):
     # the single-precision oracle performs the same IEEE operations
     d32, _ = oracle.density(p, g["sorted_pos"], g["sorted"], g["cell_start"])
     np.testing.assert_array_equal(d_gpu, d32)
-    if case == "features":
+    if case in ("features", "foam"):
         np.testing.assert_allclose(host(dye), g["dye"], rtol=1e-5, atol=1e-6)
         np.testing.assert_allclose(host(clr), g["clr"], rtol=1e-4, atol=1e-5)
 
@@ -140,10 +173,11 @@ def test_radix_sort_stable(cuda, n, bits):
 
 
 def test_stage_errors(cuda):
+    """Parameter sets the kernels do not cover are refused with a status."""
     from pibiti_gb300 import _lib
     from pibiti_gb300.sph import Scene, stage
     p = Scene.default().params
-    p.rotType = 2
+    p.bndType = 9
     with pytest.raises(_lib.SphError) as e:
         stage.set_parameters(p)
-    assert e.value.code == 4
+    assert e.value.code == 3

@@ -17,7 +17,8 @@ from pibiti_gb300.sph import ARRAY_POS, ARRAY_VEL, SPH, Scene
 pytestmark = pytest.mark.gpu
 
 DENS_RTOL = 1e-5
-CASES = ["dambreak", "truncate", "features", "bigrid", "tiny"]
+CASES = ["dambreak", "truncate", "features", "bigrid", "tiny", "rotor", "propeller", "hmapxz",
+         "hmapyz"]
 
 
 def system_from(p, pos, vel):

@@ -14,7 +14,8 @@ import pytest
 import oracle
 from conftest import params_from
 
-STEP_CASES = ["dambreak", "truncate", "features", "bigrid", "tiny"]
+STEP_CASES = ["dambreak", "truncate", "features", "bigrid", "tiny", "rotor", "propeller",
+              "hmapxz", "hmapyz"]
 
 # density: relative to the particle's density; velocity: relative to the
 # largest velocity of the case (velocities carry the whole step's update).
@@ -137,8 +138,9 @@ def test_live_reference(case, golden):
     np.testing.assert_allclose(o["vel"], r["vel"], rtol=0, atol=VEL_RTOL * np.abs(r["vel"]).max())
 
 
-def test_color_and_dye(golden):
-    g = golden("step_features.npz")
+@pytest.mark.parametrize("case", ["features", "foam"])
+def test_color_and_dye(golden, case):
+    g = golden(f"step_{case}.npz")
     p = params_from(g["params"])
     vel, dye, clr = oracle.force_color(p, g["sorted_pos"], g["sorted_vel"], g["density"],
                                        g["pressure"], g["sorted"], g["cell_start"],
