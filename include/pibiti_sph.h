@@ -233,22 +233,33 @@ int sph_mlp_adam(float* params, float* m, float* v, const float* grad, float lr,
                  float beta2, float eps, uint32_t step, void* stream);
 
 /* The learned step on a system handle.  A coarse step is one whole step
-   with the time step multiplied by `substeps` whose force pass also writes
-   16 features per particle; the MLP then adds a velocity correction
-   dv = y * out_scale * |g| * dt_coarse, and pos_factor * dv * dt_coarse to
-   the position (default pos_factor 1/2).  After every coarse step a density
-   check runs: if any scene's mean density departs from the linear
-   extrapolation of its last two accepted steps by more than `tol` times its
-   last value, or any value is not finite, the state is restored and the
-   scene set advances by `substeps` plain steps of the original time step
-   instead (counted in *fallbacks). */
+   with the time step multiplied by n = `substeps` whose force pass also
+   writes 16 features per particle; then, per particle, with v0 the velocity
+   the step started from, vs the velocity after gravity and the walls (the
+   integrate part) and v1 after the force pass:
+     dv_pre = vs - v0, dv_post = v1 - vs;
+   an optional jerk correction jerk * ((dv_pre - dv_pre') - (dv_post -
+   dv_post')) from the previous coarse step's increments (primes) of the
+   same particle; the MLP's correction dv = y * out_scale * |g| * dt_coarse;
+   and the drift correction of the position drift * dt_coarse * (v - vs -
+   dv_pre) with v the corrected velocity.  drift = (n-1)/(2n) is the
+   difference, for constant accelerations, between n steps of dt and one of
+   n dt when gravity and walls kick before the drift and the SPH force
+   after it; jerk = (n-1)/(2n) the same for accelerations linear in time.
+   After every coarse step a density check runs: if any scene's mean
+   density departs from the linear extrapolation of its last two accepted
+   steps by more than `tol` times its last value, or any value is not
+   finite, the state is restored and the scene set advances by `substeps`
+   plain steps of the original time step instead (counted in *fallbacks). */
 /* Model: FP32 parameters (host, sph_mlp_param_count() floats), feature
    mean[16] and 1/std[16] (host, 32 floats), out_scale[3]. */
 int sph_learned_set_model(SphSystem* sys, const float* params, const float* feat_stats,
                           const float* out_scale);
 int sph_learned_step(SphSystem* sys, uint32_t coarse_steps, uint32_t substeps, float tol,
                      uint32_t* fallbacks);
-int sph_learned_set_options(SphSystem* sys, float pos_factor);
+/* Factors of the drift and jerk corrections: < 0 selects (n-1)/(2n), 0
+   turns the correction off (defaults: drift (n-1)/(2n), jerk off). */
+int sph_learned_set_options(SphSystem* sys, float drift, float jerk);
 /* Training data: one coarse step (no correction) that writes the raw FP32
    features (device, N x 16, sorted order) and the original index of each
    sorted slot (device, N); the state advances by that coarse step. */

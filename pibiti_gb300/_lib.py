@@ -94,7 +94,7 @@ SIGNATURES = {
     "sph_learned_set_model": [vp, vp, vp, vp],
     "sph_learned_step": [vp, u32, u32, ctypes.c_float, P(u32)],
     "sph_features_step": [vp, u32, vp, vp],
-    "sph_learned_set_options": [vp, ctypes.c_float],
+    "sph_learned_set_options": [vp, ctypes.c_float, ctypes.c_float],
     "sph_last_error": [],
     "sph_version": [],
 }

@@ -188,7 +188,8 @@ k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
         const uint32_t* __restrict__ id, const uint32_t* __restrict__ key,
         const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
         const uint32_t* __restrict__ slot, float4* __restrict__ pos_out,
-        float4* __restrict__ vel_out, uint32_t* __restrict__ id_out) {
+        float4* __restrict__ vel_out, uint32_t* __restrict__ id_out,
+        float4* __restrict__ vel_start = nullptr) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const uint32_t c = key[i], s0 = start[c], n = count[c], me = id[i];
@@ -211,6 +212,7 @@ k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   pos_out[dest] = make_float4(x.x, x.y, x.z, x4.w);
   vel_out[dest] = make_float4(v.x, v.y, v.z, v4.w);
   id_out[dest] = me;
+  if (vel_start) vel_start[dest] = v4;  // the velocity before gravity and the walls
 }
 
 // Launch shapes of the two walks: (threads per block, minimum resident
@@ -331,7 +333,7 @@ struct FeatOut {
 };
 
 template <bool kMask, int kThreads, int kMinBlocks, bool kFeat>
-__global__ void __launch_bounds__(kThreads, kMinBlocks)
+__global__ void __launch_bounds__(kThreads, kFeat ? kMinBlocks * 3 / 2 : kMinBlocks)
 k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
         const float4* __restrict__ pos, const float4* __restrict__ vel,
         const float* __restrict__ dens, const float* __restrict__ pres,
@@ -351,6 +353,7 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   const int x0 = max(cx - 1, 0), x1 = min(cx + 1, gx - 1);
   float3 F = make_float3(0.f, 0.f, 0.f);
   FeatAcc fa;
+  const float inv_h = kFeat ? 1.f / p.h : 0.f;
   auto pair = [&](uint32_t j, float3& cell) {
     const float4 xj = __ldg(pos + j);
     const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
@@ -358,14 +361,15 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
     if (!(dist2 >= k.h2_out)) {
       const float4 vj = __ldg(vel + j);
       force_pair_near(k, vi, di, pi, vj, __ldg(dens + j), __ldg(pres + j), rx, ry, rz, dist2, cell);
-      if (kFeat) {
-        const float r = fmaxf(k.minDist, sqrtf(dist2));
+      if (kFeat) {  // network inputs (BF16): approximate reciprocals suffice
+        const float ir = rsqrtf(fmaxf(dist2, k.minDist * k.minDist));
+        const float r = fmaxf(k.minDist, dist2 * ir);
         if (r < k.h) {
-          const float q = (k.h - r) / k.h, w = q * q;
+          const float q = 1.f - r * inv_h, w = q * q;
           const float dvx = vj.x - vi.x, dvy = vj.y - vi.y, dvz = vj.z - vi.z;
           fa.sw += w;
           fa.n += 1.f;
-          fa.div += w * (dvx * rx + dvy * ry + dvz * rz) / r;
+          fa.div += w * (dvx * rx + dvy * ry + dvz * rz) * ir;
           fa.rv[0] += w * dvx;
           fa.rv[1] += w * dvy;
           fa.rv[2] += w * dvz;
@@ -491,32 +495,64 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   }
 }
 
-// The MLP's correction, sorted order: dv = y * out_scale * g * dt added to
-// the velocity and pos_factor * dv * dt to the position (pos_factor = 1/2
-// is the position change of a constant extra acceleration over the step).
+// After a coarse step of dt_c = n dt (sorted order).  Within a step,
+// gravity and the wall kicks act before the drift (integrate) and the SPH
+// force and colliders after it (the force pass).  With v0 the velocity the
+// step started from, vs the integrated velocity the force pass started
+// from and v1 its result:
+//   dv_pre  = vs - v0   (gravity and walls, evaluated at the start),
+//   dv_post = v1 - vs   (SPH force and colliders, evaluated at the end).
+// n steps of dt sample the post-drift accelerations at t + k dt, k = 1..n,
+// and the pre-drift ones at k = 0..n-1; one step of dt_c samples both once.
+// For accelerations that vary linearly in time the velocity of the n fine
+// steps differs by
+//   jerk * ((dv_pre - dv_pre') - (dv_post - dv_post')),  jerk = (n-1)/(2n),
+// (primes: the previous coarse step of the same particle, kept by original
+// index in `hist`), and for constant ones the position by
+//   drift * dt_c * (dv_post - dv_pre),  drift = (n-1)/(2n).
+// The network's correction dv = y * out_scale * |g| * dt_c (when y is
+// given) is added to the velocity and counted with dv_post in the drift.
 __global__ void k_apply_correction(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff,
                                    int S, uint32_t N, const float* __restrict__ y,
-                                   const float* __restrict__ out_scale, float pos_factor,
-                                   float4* __restrict__ pos, float4* __restrict__ vel) {
+                                   const float* __restrict__ out_scale, float drift, float jerk,
+                                   const float4* __restrict__ vel_start,
+                                   const float4* __restrict__ vel_sorted,
+                                   const uint32_t* __restrict__ id, float4* __restrict__ hist,
+                                   bool hist_valid, float4* __restrict__ pos,
+                                   float4* __restrict__ vel) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const SimParams& p = sc[S == 1 ? 0 : scene_of(poff, S, i)].p;
-  const float g = sqrtf(p.gravity.x * p.gravity.x + p.gravity.y * p.gravity.y +
-                        p.gravity.z * p.gravity.z) + 1e-6f;
-  const float u = g * p.timeStep;
-  const float dvx = y[3 * i + 0] * out_scale[0] * u, dvy = y[3 * i + 1] * out_scale[1] * u,
-              dvz = y[3 * i + 2] * out_scale[2] * u;
+  const float dt = p.timeStep;
+  const float4 vs = vel_sorted[i], v0 = vel_start[i];
   float4 v = vel[i];
-  v.x += dvx;
-  v.y += dvy;
-  v.z += dvz;
+  const float3 post = make_float3(v.x - vs.x, v.y - vs.y, v.z - vs.z);
+  const float3 pre = make_float3(vs.x - v0.x, vs.y - v0.y, vs.z - v0.z);
+  if (jerk != 0.f) {
+    const uint32_t me = id[i];
+    if (hist_valid) {
+      const float4 h = hist[me];  // previous dv_pre - dv_post
+      v.x += jerk * ((pre.x - post.x) - h.x);
+      v.y += jerk * ((pre.y - post.y) - h.y);
+      v.z += jerk * ((pre.z - post.z) - h.z);
+    }
+    hist[me] = make_float4(pre.x - post.x, pre.y - post.y, pre.z - post.z, 0.f);
+  }
+  if (y) {
+    const float g = sqrtf(p.gravity.x * p.gravity.x + p.gravity.y * p.gravity.y +
+                          p.gravity.z * p.gravity.z) + 1e-6f;
+    const float u = g * dt;
+    v.x += y[3 * i + 0] * out_scale[0] * u;
+    v.y += y[3 * i + 1] * out_scale[1] * u;
+    v.z += y[3 * i + 2] * out_scale[2] * u;
+  }
   vel[i] = v;
-  if (pos_factor != 0.f) {
-    const float k = pos_factor * p.timeStep;
+  if (drift != 0.f) {
+    const float k = drift * dt;
     float4 x = pos[i];
-    x.x += dvx * k;
-    x.y += dvy * k;
-    x.z += dvz * k;
+    x.x += k * ((v.x - vs.x) - pre.x);
+    x.y += k * ((v.y - vs.y) - pre.y);
+    x.z += k * ((v.z - vs.z) - pre.z);
     pos[i] = x;
   }
 }
@@ -565,42 +601,81 @@ __global__ void k_cell_ranges(const SceneDesc* __restrict__ sc, const uint32_t* 
   if (ce) ce[c] = n ? start[c] + n - po : kEmpty;
 }
 
-// Per scene, in double: kinetic energy, sum of density, max |rho/rho0-1|,
-// non-finite components.  Warps whose lanes share a scene reduce first.
-__global__ void k_stats(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S,
-                        uint32_t N, const float4* __restrict__ pos, const float4* __restrict__ vel,
-                        const float* __restrict__ dens, double* __restrict__ acc) {
+// Per-scene kinetic energy, density sum, max |rho/rho0 - 1| and the count
+// of non-finite coordinates.  Per-particle terms and the sum over a warp
+// are FP32 (the GPU's FP64 rate is low); warp partials are summed in FP64.
+__global__ void __launch_bounds__(kBlock) k_stats(const SceneDesc* __restrict__ sc,
+                                                  const uint32_t* __restrict__ poff, int S,
+                                                  uint32_t N, const float4* __restrict__ pos,
+                                                  const float4* __restrict__ vel,
+                                                  const float* __restrict__ dens,
+                                                  double* __restrict__ acc) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   int s = -1;
-  double ke = 0, rho = 0, dev = 0, bad = 0;
+  float ke = 0.f, rho = 0.f, dev = 0.f, bad = 0.f;
   if (i < N) {
     s = S == 1 ? 0 : scene_of(poff, S, i);
     const SimParams& p = sc[s].p;
     const float4 x = pos[i], v = vel[i];
-    const double vx = v.x, vy = v.y, vz = v.z;
-    ke = 0.5 * (double)p.particleMass * (vx * vx + vy * vy + vz * vz);
-    rho = dens ? (double)dens[i] : 0.0;
-    dev = dens ? fabs(rho / (double)p.restDensity - 1.0) : 0.0;
-    bad = (double)(!isfinite(x.x) + !isfinite(x.y) + !isfinite(x.z) + !isfinite(v.x) +
-                   !isfinite(v.y) + !isfinite(v.z));
-    if (!(ke == ke)) ke = 0;
-    if (!(dev == dev)) dev = 0;
+    ke = 0.5f * p.particleMass * (v.x * v.x + v.y * v.y + v.z * v.z);
+    rho = dens ? dens[i] : 0.f;
+    dev = dens ? fabsf(rho / p.restDensity - 1.f) : 0.f;
+    bad = (float)(!isfinite(x.x) + !isfinite(x.y) + !isfinite(x.z) + !isfinite(v.x) +
+                  !isfinite(v.y) + !isfinite(v.z));
+    if (!(ke == ke) || isinf(ke)) ke = 0.f;
+    if (!(rho == rho) || isinf(rho)) rho = 0.f;
+    if (!(dev == dev) || isinf(dev)) dev = 0.f;
+  }
+  auto warp_sum = [](float& a, float& b, float& c, float& d) {
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+      c = fmaxf(c, __shfl_xor_sync(0xffffffffu, c, o));
+      d += __shfl_xor_sync(0xffffffffu, d, o);
+    }
+  };
+  auto add = [&](int sc_, double a, double b, double c, double d) {
+    atomicAdd(acc + 4 * sc_ + 0, a);
+    atomicAdd(acc + 4 * sc_ + 1, b);
+    atomicMax((unsigned long long*)(acc + 4 * sc_ + 2), (unsigned long long)__double_as_longlong(c));
+    atomicAdd(acc + 4 * sc_ + 3, d);
+  };
+  // One scene in the whole block (always for a single scene): reduce over
+  // the block (threads past N add zeros) and add once; otherwise per warp
+  // where the warp is uniform, per thread where it is not.
+  const uint32_t first = blockIdx.x * blockDim.x;
+  const uint32_t last = min(first + blockDim.x, N) - 1;
+  const int s_first = S == 1 ? 0 : scene_of(poff, S, first);
+  if (S == 1 || s_first == scene_of(poff, S, last)) {
+    warp_sum(ke, rho, dev, bad);
+    __shared__ double part[kBlock / 32][4];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+      part[w][0] = ke;
+      part[w][1] = rho;
+      part[w][2] = dev;
+      part[w][3] = bad;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = part[0][0], b = part[0][1], c = part[0][2], d = part[0][3];
+      for (int k = 1; k < kBlock / 32; ++k) {
+        a += part[k][0];
+        b += part[k][1];
+        c = fmax(c, part[k][2]);
+        d += part[k][3];
+      }
+      add(s_first, a, b, c, d);
+    }
+    return;
   }
   const uint32_t peers = __match_any_sync(0xffffffffu, (uint32_t)s);
   if (peers == 0xffffffffu) {
-    for (int o = 16; o > 0; o >>= 1) {
-      ke += __shfl_xor_sync(0xffffffffu, ke, o);
-      rho += __shfl_xor_sync(0xffffffffu, rho, o);
-      dev = fmax(dev, __shfl_xor_sync(0xffffffffu, dev, o));
-      bad += __shfl_xor_sync(0xffffffffu, bad, o);
-    }
+    warp_sum(ke, rho, dev, bad);
     if ((threadIdx.x & 31) != 0) return;
   }
   if (s < 0) return;
-  atomicAdd(acc + 4 * s + 0, ke);
-  atomicAdd(acc + 4 * s + 1, rho);
-  atomicMax((unsigned long long*)(acc + 4 * s + 2), (unsigned long long)__double_as_longlong(dev));
-  atomicAdd(acc + 4 * s + 3, bad);
+  add(s, ke, rho, dev, bad);
 }
 
 }  // namespace
@@ -643,12 +718,17 @@ struct SphSystem {
   void* mlp_img = nullptr;           // packed BF16 weights
   float* mlp_aux = nullptr;          // feature mean[16], inv_std[16], out_scale[3]
   bool model_set = false;
-  float pos_factor = 0.5f;           // position part of the correction
+  float drift = -1.f;                // drift correction factor; < 0: (n-1)/(2n)
+  float jerk = 0.f;                  // jerk correction factor; < 0: (n-1)/(2n)
+  float4* vstart = nullptr;          // pre-integrate velocity of the coarse step (sorted)
+  float4* hist = nullptr;            // per original index: previous dv_pre - dv_post
+  bool hist_valid = false;
   uint16_t* feat = nullptr;          // N x 16 standardised features (BF16)
   float* mlp_y = nullptr;            // N x 3 corrections
-  float4* bk_pos = nullptr;          // checkpoint for the fallback
-  float4* bk_vel = nullptr;
-  uint32_t* bk_id = nullptr;
+  float4* bk_vel = nullptr;          // velocity checkpoint for the fallback
+  double* stats_host = nullptr;      // pinned, 4 per scene
+  std::vector<double> lr_ref[2];     // mean densities of the last two accepted steps
+  int lr_refs = 0;                   // how many of lr_ref are valid for the current state
 };
 
 namespace {
@@ -681,6 +761,7 @@ struct StepOpts {
   const SceneDesc* scenes = nullptr;  // scene table (fine or coarse time step)
   bool feat = false;                  // force pass also writes learned-corrector features
   FeatOut fo = {nullptr, nullptr, nullptr};
+  float4* vel_start = nullptr;        // k_place also writes the pre-integrate velocity
 };
 
 template <bool kMask, int kThreads, int kMinBlocks, class Mark>
@@ -740,7 +821,7 @@ int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr,
   mark();
   k_place<<<gN, kBlock, 0, st>>>(sc, s->d_poff, s->S, s->N, s->pos[a], s->vel[v], s->id[a],
                                  s->key, s->start, s->count, s->slot, s->pos[b], s->vel[1 - v],
-                                 s->id[b]);
+                                 s->id[b], o.vel_start);
   mark();
   if (s->masks)
     launch_walks<true>(s, st, b, v, o, mark);
@@ -778,11 +859,12 @@ void free_all(SphSystem* s) {
   void* bufs[] = {s->d_scenes, s->d_poff, s->d_coff, s->pos[0], s->pos[1], s->vel[0], s->vel[1],
                   s->id[0], s->id[1], s->key, s->rank, s->slot, s->count, s->start, s->scan_tmp,
                   s->dens, s->pres, s->masks, s->flags, s->stats, s->staging, s->d_coarse,
-                  s->mlp_img, s->mlp_aux, s->feat, s->mlp_y, s->bk_pos, s->bk_vel, s->bk_id,
+                  s->mlp_img, s->mlp_aux, s->feat, s->mlp_y, s->bk_vel, s->vstart, s->hist,
                   s->big_list, s->big_count, s->sort_scratch};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+  if (s->stats_host) cudaFreeHost(s->stats_host);
 }
 
 template <class T>
@@ -926,6 +1008,7 @@ int sph_set_stream(SphSystem* s, void* stream) {
 
 int sph_set_params(SphSystem* s, uint32_t scene, const SimParams* p) {
   if (!s || !p || scene >= (uint32_t)s->S) return fail(SPH_ERR_ARG, "set_params: bad arguments");
+  s->lr_refs = 0;  // the learned step's density history no longer applies
   const SimParams& o = s->params[scene];
   if (p->numParticles != o.numParticles || p->numCells != o.numCells ||
       p->gridSize.x != o.gridSize.x || p->gridSize.y != o.gridSize.y || p->gridSize.z != o.gridSize.z)
@@ -951,6 +1034,7 @@ uint32_t sph_scene_offset(const SphSystem* s, uint32_t scene) {
 int sph_set_array(SphSystem* s, uint32_t which, const sph_float4* data, uint32_t start,
                   uint32_t count, int src_on_device) {
   if (!s || !data || which > SPH_ARRAY_VEL) return fail(SPH_ERR_ARG, "set_array: bad arguments");
+  s->lr_refs = 0;  // the learned step's density history no longer applies
   if ((uint64_t)start + count > s->N) return fail(SPH_ERR_ARG, "set_array: range beyond %u particles", s->N);
   if (count == 0) return SPH_OK;
   SPH_TRY(ensure_staging(s));
@@ -985,6 +1069,7 @@ int sph_get_array(SphSystem* s, uint32_t which, sph_float4* out, int dst_on_devi
 
 int sph_step(SphSystem* s, uint32_t steps) {
   if (!s) return fail(SPH_ERR_ARG, "null handle");
+  s->lr_refs = 0;  // the learned step's density history no longer applies
   uint32_t done = 0;
   const uint32_t gs = s->graph_steps;
   if (steps >= gs) {
@@ -1023,6 +1108,7 @@ int sph_get_walk_shape(SphSystem* s, uint32_t* shape, uint32_t* threads) {
 
 int sph_autotune(SphSystem* s, uint32_t trial_steps, float* ms_per_step, uint32_t* chosen) {
   if (!s || trial_steps == 0) return fail(SPH_ERR_ARG, "autotune: bad arguments");
+  s->lr_refs = 0;  // the learned step's density history no longer applies
   SPH_CUDA(cudaStreamSynchronize(s->stream), "autotune: drain");
   // Save the state so that tuning leaves the simulation where it was.
   float4 *sp = nullptr, *sv = nullptr;
@@ -1130,14 +1216,17 @@ int sph_learned_set_model(SphSystem* s, const float* params, const float* feat_s
   return rc;
 }
 
-int sph_learned_set_options(SphSystem* s, float pos_factor) {
-  if (!s || !(pos_factor == pos_factor)) return fail(SPH_ERR_ARG, "learned_set_options: bad arguments");
-  s->pos_factor = pos_factor;
+int sph_learned_set_options(SphSystem* s, float drift, float jerk) {
+  if (!s || !(drift == drift) || !(jerk == jerk))
+    return fail(SPH_ERR_ARG, "learned_set_options: bad arguments");
+  s->drift = drift;
+  s->jerk = jerk;
   return SPH_OK;
 }
 
 int sph_features_step(SphSystem* s, uint32_t substeps, float* feat_raw, uint32_t* ids) {
   if (!s || substeps == 0) return fail(SPH_ERR_ARG, "features_step: bad arguments");
+  s->lr_refs = 0;  // the learned step's density history no longer applies
   if (s->coarse_sub != substeps) SPH_TRY(ensure_coarse(s, substeps));
   StepOpts o;
   o.scenes = s->d_coarse;
@@ -1157,31 +1246,36 @@ int sph_learned_step(SphSystem* s, uint32_t coarse_steps, uint32_t substeps, flo
   if (s->coarse_sub != substeps) SPH_TRY(ensure_coarse(s, substeps));
   if (!s->feat) SPH_TRY(dalloc(&s->feat, (size_t)16 * s->N, "features"));
   if (!s->mlp_y) SPH_TRY(dalloc(&s->mlp_y, (size_t)3 * s->N, "corrections"));
-  if (!s->bk_pos) SPH_TRY(dalloc(&s->bk_pos, s->N, "checkpoint"));
   if (!s->bk_vel) SPH_TRY(dalloc(&s->bk_vel, s->N, "checkpoint"));
-  if (!s->bk_id) SPH_TRY(dalloc(&s->bk_id, s->N, "checkpoint"));
-  std::vector<double> st, ref, ref2;
-  bool have_ref = false, have_ref2 = false;
-  if (s->stepped) {
-    SPH_TRY(scene_stats(s, ref));
-    have_ref = true;
+  if (!s->vstart) SPH_TRY(dalloc(&s->vstart, s->N, "coarse start velocity"));
+  if (!s->hist) SPH_TRY(dalloc(&s->hist, s->N, "coarse increments"));
+  if (s->lr_refs == 0) s->hist_valid = false;
+  std::vector<double> st;
+  if (s->lr_refs == 0 && s->stepped) {
+    SPH_TRY(scene_stats(s, s->lr_ref[0]));
+    s->lr_refs = 1;
   }
   uint32_t fb = 0;
+  const float auto_f = (float)(substeps - 1) / (2.f * (float)substeps);
+  const float drift = s->drift < 0.f ? auto_f : s->drift;
+  const float jerk = s->jerk < 0.f ? auto_f : s->jerk;
   StepOpts o;
   o.scenes = s->d_coarse;
+  o.vel_start = s->vstart;
   o.feat = true;
   o.fo = {nullptr, s->feat, s->mlp_aux};
   for (uint32_t k = 0; k < coarse_steps; ++k) {
+    // A step reads pos[cp] and id[cp] and writes the other pair, so only
+    // the velocity (overwritten by the force pass) needs a checkpoint.
     const int cp0 = s->cp, cv0 = s->cv;
-    SPH_CUDA(cudaMemcpyAsync(s->bk_pos, s->pos[cp0], sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream), "checkpoint");
     SPH_CUDA(cudaMemcpyAsync(s->bk_vel, s->vel[cv0], sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream), "checkpoint");
-    SPH_CUDA(cudaMemcpyAsync(s->bk_id, s->id[cp0], sizeof(uint32_t) * s->N, cudaMemcpyDeviceToDevice, s->stream), "checkpoint");
     SPH_TRY(enqueue_step(s, s->stream, nullptr, &o));
     SPH_TRY(sph_mlp_forward(s->mlp_img, s->feat, s->N, s->mlp_y, s->stream));
     k_apply_correction<<<grid_for(s->N, kBlock), kBlock, 0, s->stream>>>(
-        s->d_coarse, s->d_poff, s->S, s->N, s->mlp_y, s->mlp_aux + 32, s->pos_factor,
-        s->pos[s->cp], s->vel[s->cv]);
+        s->d_coarse, s->d_poff, s->S, s->N, s->mlp_y, s->mlp_aux + 32, drift, jerk, s->vstart,
+        s->vel[1 - s->cv], s->id[s->cp], s->hist, s->hist_valid, s->pos[s->cp], s->vel[s->cv]);
     SPH_CUDA(cudaGetLastError(), "apply correction");
+    s->hist_valid = jerk != 0.f;
     // density-deviation check, per scene: the mean density of the step may
     // depart from the linear extrapolation of the last two accepted steps
     // by at most tol (relative), and nothing may be NaN/Inf
@@ -1189,9 +1283,9 @@ int sph_learned_step(SphSystem* s, uint32_t coarse_steps, uint32_t substeps, flo
     bool ok = true;
     for (int i = 0; i < s->S && ok; ++i) {
       if (st[4 * i + 3] != 0.0 || !(st[4 * i + 1] == st[4 * i + 1])) ok = false;
-      if (have_ref && ok) {
-        const double r1 = ref[4 * i + 1];
-        const double pred = have_ref2 ? 2.0 * r1 - ref2[4 * i + 1] : r1;
+      if (s->lr_refs > 0 && ok) {
+        const double r1 = s->lr_ref[0][4 * i + 1];
+        const double pred = s->lr_refs > 1 ? 2.0 * r1 - s->lr_ref[1][4 * i + 1] : r1;
         if (!(fabs(st[4 * i + 1] - pred) <= tol * r1)) ok = false;
       }
     }
@@ -1199,16 +1293,14 @@ int sph_learned_step(SphSystem* s, uint32_t coarse_steps, uint32_t substeps, flo
       ++fb;
       s->cp = cp0;
       s->cv = cv0;
-      SPH_CUDA(cudaMemcpyAsync(s->pos[cp0], s->bk_pos, sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream), "restore");
+      s->hist_valid = false;
       SPH_CUDA(cudaMemcpyAsync(s->vel[cv0], s->bk_vel, sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream), "restore");
-      SPH_CUDA(cudaMemcpyAsync(s->id[cp0], s->bk_id, sizeof(uint32_t) * s->N, cudaMemcpyDeviceToDevice, s->stream), "restore");
       for (uint32_t q = 0; q < substeps; ++q) SPH_TRY(enqueue_step(s, s->stream));
       SPH_TRY(scene_stats(s, st));
     }
-    ref2 = ref;
-    have_ref2 = have_ref;
-    ref = st;
-    have_ref = true;
+    s->lr_ref[1].swap(s->lr_ref[0]);
+    s->lr_ref[0] = st;
+    s->lr_refs = s->lr_refs < 2 ? s->lr_refs + 1 : 2;
   }
   if (fallbacks) *fallbacks = fb;
   return SPH_OK;
@@ -1289,9 +1381,12 @@ int sph_stats(SphSystem* s, double* out) {
                                                             s->pos[s->cp], s->vel[s->cv],
                                                             s->stepped ? s->dens : nullptr, s->stats);
   SPH_CUDA(cudaGetLastError(), "stats kernel");
-  SPH_CUDA(cudaMemcpyAsync(out, s->stats, sizeof(double) * 4 * s->S, cudaMemcpyDeviceToHost, s->stream),
-           "stats copy");
+  if (!s->stats_host)
+    SPH_CUDA(cudaMallocHost((void**)&s->stats_host, sizeof(double) * 4 * s->S), "stats host buffer");
+  SPH_CUDA(cudaMemcpyAsync(s->stats_host, s->stats, sizeof(double) * 4 * s->S,
+                           cudaMemcpyDeviceToHost, s->stream), "stats copy");
   SPH_CUDA(cudaStreamSynchronize(s->stream), "stats sync");
+  memcpy(out, s->stats_host, sizeof(double) * 4 * s->S);
   for (int i = 0; i < s->S; ++i) {
     const double n = s->poff[i + 1] - s->poff[i];
     out[4 * i + 1] = n ? out[4 * i + 1] / n : 0.0;

@@ -71,9 +71,10 @@ def learned_step(sph: SPH, coarse_steps: int, substeps: int = SUBSTEPS, tol: flo
     return fb.value
 
 
-def set_options(sph: SPH, pos_factor: float = 0.5) -> None:
-    """Position part of the correction (pos_factor * dv * dt_coarse)."""
-    _lib.check(_lib.lib().sph_learned_set_options(sph._h, pos_factor))
+def set_options(sph: SPH, drift: float = -1.0, jerk: float = 0.0) -> None:
+    """Factors of the coarse step's drift (position) and jerk (velocity)
+    corrections: negative for (n-1)/(2n), 0 for none."""
+    _lib.check(_lib.lib().sph_learned_set_options(sph._h, drift, jerk))
 
 
 def features_step(sph: SPH, feat, ids, substeps: int = SUBSTEPS) -> None:
@@ -128,6 +129,24 @@ def generate(xmls, pos, vel, sizes, snapshots: int = 8, warm: int = 20, gap: int
     return torch.cat(feats), torch.cat(targets)
 
 
+# Snapshot phases of the shipped model's training data: (snapshots, warm-up
+# steps, steps between snapshots) of the fine run; the first covers the
+# early collapse of each dam break, the second the rest of 2000 steps.
+PHASES = ((6, 20, 30), (9, 220, 200))
+
+
+def generate_phases(xmls, pos, vel, sizes, phases=PHASES, substeps: int = SUBSTEPS):
+    """generate() over several snapshot phases, concatenated."""
+    import torch
+    fs, ts = [], []
+    for snaps, warm, gap in phases:
+        f, t = generate(xmls, pos, vel, sizes, snapshots=snaps, warm=warm, gap=gap,
+                        substeps=substeps)
+        fs.append(f)
+        ts.append(t)
+    return torch.cat(fs), torch.cat(ts)
+
+
 def train(feats, targets, epochs: int = 6, batch: int = 65536, lr: float = 2e-3, seed: int = 0,
           log=None) -> Model:
     """Adam on the project's MLP kernels; returns the trained model."""
@@ -177,38 +196,53 @@ def train(feats, targets, epochs: int = 6, batch: int = 65536, lr: float = 2e-3,
                  out_scale.cpu().numpy(), {"loss_history": history, "samples": int(n)})
 
 
+def zero_model() -> Model:
+    """A network whose output is zero: the learned step then reduces to the
+    coarse step with the drift correction and the density check."""
+    return Model(np.zeros(_lib.lib().sph_mlp_param_count(), np.float32), np.zeros(16, np.float32),
+                 np.ones(16, np.float32), np.ones(3, np.float32), {"zero": True})
+
+
 def one_step_errors(model: Model, xml: str, pos, vel, warm: int = 40,
                     substeps: int = SUBSTEPS) -> dict:
-    """Velocity error of one coarse step, with and without the network,
-    against `substeps` fine steps from the same state (mean |dv| over
-    particles, in m/s)."""
-    import torch
+    """Errors of one coarse step against `substeps` fine steps from the same
+    state: mean |dv| (m/s) and mean |dx| (m) over particles, for the coarse
+    step alone, with the drift correction, and with drift and network."""
     p = Scene.parse(xml).params
-    with SPH(p) as fine, SPH(p) as plain, SPH(p) as lrn:
+    pc = p.copy()
+    pc.timeStep = p.timeStep * substeps
+    with SPH(p) as fine:
         fine.set_array(ARRAY_POS, pos)
         fine.set_array(ARRAY_VEL, vel)
         fine.update(warm)
         s_pos, s_vel = fine.get_array(ARRAY_POS), fine.get_array(ARRAY_VEL)
-        for h in (plain, lrn):
+        fine.update(substeps)
+        xf, vf = fine.get_array(ARRAY_POS), fine.get_array(ARRAY_VEL)
+    out = {}
+    for name in ("coarse", "drift", "learned"):
+        with SPH(pc if name == "coarse" else p) as h:
             h.set_array(ARRAY_POS, s_pos)
             h.set_array(ARRAY_VEL, s_vel)
-        fine.update(substeps)
-        f = torch.empty((fine.n, 16), dtype=torch.float32, device="cuda")
-        ids = torch.empty(fine.n, dtype=torch.int32, device="cuda")
-        features_step(plain, f, ids, substeps)
-        model.install(lrn)
-        fb = learned_step(lrn, 1, substeps, tol=1e9)
-        vf, vp, vl = fine.get_array(ARRAY_VEL), plain.get_array(ARRAY_VEL), lrn.get_array(ARRAY_VEL)
-    e_plain = float(np.abs(vp[:, :3] - vf[:, :3]).sum(1).mean())
-    e_learned = float(np.abs(vl[:, :3] - vf[:, :3]).sum(1).mean())
-    return {"coarse_plain": e_plain, "coarse_learned": e_learned, "fallbacks": fb}
+            if name == "coarse":
+                h.update(1)
+            else:
+                (model if name == "learned" else zero_model()).install(h)
+                learned_step(h, 1, substeps, tol=1e9)
+            x, v = h.get_array(ARRAY_POS), h.get_array(ARRAY_VEL)
+        out[f"dv_{name}"] = float(np.abs(v[:, :3] - vf[:, :3]).sum(1).mean())
+        out[f"dx_{name}"] = float(np.abs(x[:, :3] - xf[:, :3]).sum(1).mean())
+    return out
 
 
 def rollout(model: Model, xml: str, pos, vel, fine_steps: int, substeps: int = SUBSTEPS,
-            tol: float = 0.01, warm: int = 0, pos_factor: float = 0.5) -> dict:
-    """Mean-density trajectories of the fine-dt plain run, the coarse run
-    without the network and the learned run, sampled every `substeps` fine
-    steps; errors relative to the fine run, and the wall time of each."""
+            tol: float = 0.01, warm: int = 0, drift: float = -1.0, jerk: float = 0.0,
+            trace: int = 0) -> dict:
+    """Mean-density trajectories of the fine-dt plain run, the coarse run,
+    the coarse run with the drift correction (no network, no check) and the
+    learned run, sampled every `substeps` fine steps.  Errors are relative to
+    the fine run (max and mean over the samples); times are wall clock of
+    the fine and the learned run, each including one stats read per sample.
+    With trace = k, every k-th sample of each relative error is returned too."""
     import torch
     p = Scene.parse(xml).params
     pc = p.copy()
@@ -228,32 +262,48 @@ def rollout(model: Model, xml: str, pos, vel, fine_steps: int, substeps: int = S
             fine.update(substeps)
             rho_f.append(fine.stats()[0][1])
         out["fine_s"] = time.perf_counter() - t0
+    rho = {}
     with SPH(pc) as c:
         c.set_array(ARRAY_POS, s_pos)
         c.set_array(ARRAY_VEL, s_vel)
-        rho_c = []
+        rho["coarse"] = []
         for _ in range(coarse_steps):
             c.update(1)
-            rho_c.append(c.stats()[0][1])
+            rho["coarse"].append(c.stats()[0][1])
+    with SPH(p) as d:
+        d.set_array(ARRAY_POS, s_pos)
+        d.set_array(ARRAY_VEL, s_vel)
+        zero_model().install(d)
+        set_options(d, drift, jerk)
+        rho["drift"] = []
+        for _ in range(coarse_steps):
+            learned_step(d, 1, substeps, 1e9)
+            rho["drift"].append(d.stats()[0][1])
     with SPH(p) as lrn:
         lrn.set_array(ARRAY_POS, s_pos)
         lrn.set_array(ARRAY_VEL, s_vel)
         model.install(lrn)
-        set_options(lrn, pos_factor)
-        rho_l, fb = [], 0
+        set_options(lrn, drift, jerk)
+        learned_step(lrn, 0, substeps, tol)  # allocations outside the timed loop
+        rho["learned"], fb = [], 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(coarse_steps):
             fb += learned_step(lrn, 1, substeps, tol)
-            rho_l.append(lrn.stats()[0][1])
+            rho["learned"].append(lrn.stats()[0][1])
         out["learned_s"] = time.perf_counter() - t0
-    rho_f, rho_c, rho_l = map(np.asarray, (rho_f, rho_c, rho_l))
-    out.update({
-        "err_coarse_plain": float(np.max(np.abs(rho_c - rho_f) / rho_f)),
-        "err_learned": float(np.max(np.abs(rho_l - rho_f) / rho_f)),
-        "fallbacks": int(fb), "coarse_steps": coarse_steps,
-        "rho_fine_end": float(rho_f[-1]), "rho_learned_end": float(rho_l[-1]),
-    })
+    rho_f = np.asarray(rho_f)
+    if trace:
+        out["trace_rho_fine"] = [round(float(x), 3) for x in rho_f[trace - 1::trace]]
+    for k, r in rho.items():
+        e = np.abs(np.asarray(r) - rho_f) / rho_f
+        out[f"err_{k}_max"] = float(e.max())
+        out[f"err_{k}_mean"] = float(e.mean())
+        if trace:
+            out[f"trace_{k}"] = [round(float(x), 5) for x in e[trace - 1::trace]]
+    out.update({"fallbacks": int(fb), "coarse_steps": coarse_steps,
+                "speedup": out["fine_s"] / out["learned_s"],
+                "rho_fine_end": float(rho_f[-1]), "rho_learned_end": float(rho["learned"][-1])})
     return out
 
 
@@ -267,9 +317,9 @@ def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("cmd", choices=["train", "evaluate"])
     ap.add_argument("--scenes", type=int, default=256)
-    ap.add_argument("--snapshots", type=int, default=6)
-    ap.add_argument("--epochs", type=int, default=8)
-    ap.add_argument("--fine-steps", type=int, default=400)
+    ap.add_argument("--epochs", type=int, default=16)
+    ap.add_argument("--batch", type=int, default=32768)
+    ap.add_argument("--fine-steps", type=int, default=2000)
     ap.add_argument("--model", default=MODEL_PATH)
     a = ap.parse_args(argv)
     log = lambda *m: print(*m, file=sys.stderr, flush=True)  # noqa: E731
@@ -277,14 +327,14 @@ def main(argv=None) -> int:
     if a.cmd == "train":
         e = configs.ensemble(scenes=a.scenes)
         t0 = time.perf_counter()
-        f, t = generate(e.xmls, e.pos, e.vel, e.sizes, snapshots=a.snapshots)
+        f, t = generate_phases(e.xmls, e.pos, e.vel, e.sizes)
         log(f"generated {f.shape[0]} samples in {time.perf_counter() - t0:.1f} s")
         t0 = time.perf_counter()
-        model = train(f, t, epochs=a.epochs, log=log)
-        model.info.update({"scenes": a.scenes, "snapshots": a.snapshots, "epochs": a.epochs,
-                           "train_s": time.perf_counter() - t0})
+        model = train(f, t, epochs=a.epochs, batch=a.batch, log=log)
+        model.info.update({"scenes": a.scenes, "phases": PHASES, "epochs": a.epochs,
+                           "batch": a.batch, "train_s": time.perf_counter() - t0})
         model.save(a.model)
-        w = configs.dambreak_small(side=32)
+        w = configs.dambreak_small(side=32, seed=9)
         print(json.dumps({"trained": model.info,
                           "one_step_32k": one_step_errors(model, w.xml, w.pos, w.vel)}))
     else:
