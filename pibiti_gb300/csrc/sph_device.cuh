@@ -251,27 +251,32 @@ __device__ __forceinline__ ForceConsts force_consts(const SimParams& p) {
   return k;
 }
 
-__device__ __forceinline__ void force_pair_near(const ForceConsts& k, float4 vi, float di, float pi,
-                                                float4 vj, float dj, float pj, float rx, float ry,
-                                                float rz, float dist2, float3& acc);
+__device__ __forceinline__ void force_pair_near(const ForceConsts& k, float4 vi, float inv_di,
+                                                float pi, float4 vj, float inv_dj, float pj,
+                                                float rx, float ry, float rz, float dist2,
+                                                float3& acc);
 
 // compForceCell inner step + compForcePair (Kernel_Cell.cui:210-228,
 // 251-258): d12 = min(minDens, 1/(rho_i rho_j)); r = max(minDist, |x_i-x_j|);
 // if r < h: F += (c Spiky (p_i+p_j)/r (x_i-x_j) + Lap mu (v_j-v_i)) c d12.
-__device__ __forceinline__ void force_pair(const ForceConsts& k, float4 xi, float4 vi, float di,
-                                           float pi, float4 xj, float4 vj, float dj, float pj,
+// 1/(rho_i rho_j) is formed as (1/rho_i)(1/rho_j) from the correctly
+// rounded reciprocals, so that a walk computes one per particle and none
+// per pair (within 2 ulp of the reference's single division).
+__device__ __forceinline__ void force_pair(const ForceConsts& k, float4 xi, float4 vi, float inv_di,
+                                           float pi, float4 xj, float4 vj, float inv_dj, float pj,
                                            float3& acc) {
   const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
   const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
-  force_pair_near(k, vi, di, pi, vj, dj, pj, rx, ry, rz, dist2, acc);
+  force_pair_near(k, vi, inv_di, pi, vj, inv_dj, pj, rx, ry, rz, dist2, acc);
 }
 
 // The part of force_pair after the squared distance; the fused walk calls it
 // only for candidates not excluded by ForceConsts::h2_out (and for NaN).
-__device__ __forceinline__ void force_pair_near(const ForceConsts& k, float4 vi, float di, float pi,
-                                                float4 vj, float dj, float pj, float rx, float ry,
-                                                float rz, float dist2, float3& acc) {
-  const float dd = __fdiv_rn(1.0f, __fmul_rn(di, dj));
+__device__ __forceinline__ void force_pair_near(const ForceConsts& k, float4 vi, float inv_di,
+                                                float pi, float4 vj, float inv_dj, float pj,
+                                                float rx, float ry, float rz, float dist2,
+                                                float3& acc) {
+  const float dd = __fmul_rn(inv_di, inv_dj);
   const float d12 = fminf(k.minDens, dd);
   const float vx = __fsub_rn(vj.x, vi.x), vy = __fsub_rn(vj.y, vi.y), vz = __fsub_rn(vj.z, vi.z);
   const float r = fmaxf(k.minDist, __fsqrt_rn(dist2));

@@ -172,7 +172,7 @@ __global__ void st_force(const SimParams p, const float4* __restrict__ spos,
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 xi = spos[i], vi = svel[i];
-  const float pi = pressure[i], di = density[i];
+  const float pi = pressure[i], di = density[i], inv_di = __frcp_rn(di);
   const int3 g = grid_pos(p, xi);
   const ForceConsts k = force_consts(p);
   float3 F = make_float3(0.f, 0.f, 0.f);
@@ -186,7 +186,9 @@ __global__ void st_force(const SimParams p, const float4* __restrict__ spos,
         for (uint32_t q = 0; q < p.maxParInCell; ++q) {
           const uint32_t j = start + q;
           if (j >= n || ref_key(hash, n, j) != gh) break;
-          if (j != i) force_pair(k, xi, vi, di, pi, spos[j], svel[j], density[j], pressure[j], cell);
+          if (j != i)
+            force_pair(k, xi, vi, inv_di, pi, spos[j], svel[j], __frcp_rn(density[j]), pressure[j],
+                       cell);
         }
         F.x = __fadd_rn(F.x, cell.x);
         F.y = __fadd_rn(F.y, cell.y);

@@ -18,6 +18,9 @@
 //                      take a rank in the cell with one atomic per warp group
 //   exclusive scan     count -> start
 //   k_scatter_ids      slot[start + rank] = original index
+//   k_find_cells,      the id segments of cells with more than 32 particles
+//   k_sort_cells,      sorted (a warp, a block, or a block over global
+//   k_sort_big_cells   scratch, by size)
 //   k_place            stable position inside the cell = number of smaller
 //                      original indices there (the reference's sort is
 //                      stable on original order); integrate again and write
@@ -133,20 +136,40 @@ __device__ __forceinline__ void bitonic(uint32_t* buf, uint32_t m, uint32_t me, 
     }
 }
 
+// Cells that need their id segment sorted: each warp reads 32 counts at
+// once; cells above kLinearRank go to `list` (<= kWarpSortMax) or
+// `big_list`, appended with one atomic per warp and list.
+__global__ void k_find_cells(uint32_t C, const uint32_t* __restrict__ count,
+                             uint32_t* __restrict__ list, uint32_t* __restrict__ counters,
+                             uint32_t* __restrict__ big_list) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t n = c < C ? count[c] : 0u;
+  const bool mid = n > kLinearRank && n <= kWarpSortMax, big = n > kWarpSortMax;
+  const uint32_t bm = __ballot_sync(0xffffffffu, mid), bb = __ballot_sync(0xffffffffu, big);
+  uint32_t base_m = 0, base_b = 0;
+  if (lane == 0) {
+    if (bm) base_m = atomicAdd(counters + 0, (uint32_t)__popc(bm));
+    if (bb) base_b = atomicAdd(counters + 1, (uint32_t)__popc(bb));
+  }
+  base_m = __shfl_sync(0xffffffffu, base_m, 0);
+  base_b = __shfl_sync(0xffffffffu, base_b, 0);
+  const uint32_t below = (1u << lane) - 1u;
+  if (mid) list[base_m + (uint32_t)__popc(bm & below)] = c;
+  if (big) big_list[base_b + (uint32_t)__popc(bb & below)] = c;
+}
+
+// One warp per listed cell (grid-stride over the list): bitonic sort of
+// the segment in shared memory.
 __global__ void __launch_bounds__(kSortWarps * 32)
-k_sort_cells(uint32_t C, const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
-             uint32_t* __restrict__ slot, uint32_t* __restrict__ big_list,
-             uint32_t* __restrict__ big_count) {
+k_sort_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
+             uint32_t* __restrict__ slot, const uint32_t* __restrict__ list,
+             const uint32_t* __restrict__ counters) {
   __shared__ uint32_t buf[kSortWarps][kWarpSortMax];
   const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (uint32_t c = blockIdx.x * kSortWarps + w; c < C; c += gridDim.x * kSortWarps) {
-    const uint32_t n = count[c];
-    if (n <= kLinearRank) continue;
-    if (n > kWarpSortMax) {
-      if (lane == 0) big_list[atomicAdd(big_count, 1u)] = c;
-      continue;
-    }
-    const uint32_t s0 = start[c], m = pow2_at_least(n);
+  const uint32_t nl = counters[0];
+  for (uint32_t q = blockIdx.x * kSortWarps + w; q < nl; q += gridDim.x * kSortWarps) {
+    const uint32_t c = list[q], n = count[c], s0 = start[c], m = pow2_at_least(n);
     uint32_t* b = buf[w];
     for (uint32_t k = lane; k < m; k += 32) b[k] = k < n ? slot[s0 + k] : 0xffffffffu;
     __syncwarp();
@@ -245,8 +268,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 k_density(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
           const float4* __restrict__ pos, const uint32_t* __restrict__ start,
           const uint32_t* __restrict__ count, float* __restrict__ dens_out,
-          float* __restrict__ pres_out, unsigned long long* __restrict__ masks,
-          uint32_t* __restrict__ flags) {
+          float* __restrict__ pres_out, float2* __restrict__ dp_out,
+          unsigned long long* __restrict__ masks, uint32_t* __restrict__ flags) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
@@ -278,6 +301,8 @@ k_density(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, i
         const uint32_t s0 = __ldg(start + c);
         float cell = 0.f;
         uint32_t m = 0;
+        // only the particle's own cell holds i
+        const uint32_t self = (r == 4 && x == cx) ? i - s0 : 0xffffffffu;
         auto cand = [&](uint32_t k) {
           const float4 xj = __ldg(pos + s0 + k);
           const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
@@ -288,8 +313,6 @@ k_density(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, i
           }
           if (kMask && !(r2 >= h2_out)) m |= 1u << k;
         };
-        // only the particle's own cell holds i
-        const uint32_t self = (r == 4 && x == cx) ? i - s0 : 0xffffffffu;
         if (self < n) {
 #pragma unroll 4
           for (uint32_t k = 0; k < self; ++k) cand(k);
@@ -308,8 +331,10 @@ k_density(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, i
   }
   if (trunc) atomicOr(flags, 1u);
   const float dens = __fmul_rn(__fmul_rn(sum, p.Poly6Kern), p.particleMass);
+  const float pres = __fmul_rn(__fsub_rn(dens, p.restDensity), p.stiffness);
   dens_out[i] = dens;
-  pres_out[i] = __fmul_rn(__fsub_rn(dens, p.restDensity), p.stiffness);
+  pres_out[i] = pres;
+  dp_out[i] = make_float2(__frcp_rn(dens), pres);  // the force pass's per-neighbour record
 }
 
 // Learned-corrector features of particle i (SPH_MLP_IN = 16), from the
@@ -333,10 +358,10 @@ struct FeatOut {
 };
 
 template <bool kMask, int kThreads, int kMinBlocks, bool kFeat>
-__global__ void __launch_bounds__(kThreads, kFeat ? kMinBlocks * 3 / 2 : kMinBlocks)
+__global__ void __launch_bounds__(kThreads, kFeat ? kMinBlocks * 3 / 4 : kMinBlocks)
 k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
         const float4* __restrict__ pos, const float4* __restrict__ vel,
-        const float* __restrict__ dens, const float* __restrict__ pres,
+        const float* __restrict__ dens, const float2* __restrict__ dp,
         const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
         const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out, FeatOut fo) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -344,7 +369,8 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
   const SimParams& p = d.p;
   const float4 xi = pos[i], vi = vel[i];
-  const float di = dens[i], pi = pres[i];
+  const float2 dpi = dp[i];
+  const float inv_di = dpi.x, pi = dpi.y;
   const ForceConsts k = force_consts(p);
   const int3 g = grid_pos(p, xi);
   const int gx = (int)p.gridSize.x, gy = (int)p.gridSize.y, gz = (int)p.gridSize.z;
@@ -360,7 +386,8 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
     const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
     if (!(dist2 >= k.h2_out)) {
       const float4 vj = __ldg(vel + j);
-      force_pair_near(k, vi, di, pi, vj, __ldg(dens + j), __ldg(pres + j), rx, ry, rz, dist2, cell);
+      const float2 dpj = __ldg(dp + j);
+      force_pair_near(k, vi, inv_di, pi, vj, dpj.x, dpj.y, rx, ry, rz, dist2, cell);
       if (kFeat) {  // network inputs (BF16): approximate reciprocals suffice
         const float ir = rsqrtf(fmaxf(dist2, k.minDist * k.minDist));
         const float r = fmaxf(k.minDist, dist2 * ir);
@@ -388,44 +415,36 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
     cell = make_float3(0.f, 0.f, 0.f);
   };
   if (kMask) {
-    // One loop over every set bit of all 9 row masks, in walk order, so a
-    // warp runs max(per-thread neighbour count) iterations rather than the
-    // sum over cells of per-cell maxima.  Cell partial sums are flushed
-    // into F when the cell changes; skipped (zero) partials leave F as is.
-    int r = -1, cur = -1;
-    unsigned long long m = 0;
-    uint32_t s0 = 0, s1 = 0, s2 = 0, b1 = 0, b2 = 0;
-    for (;;) {
-      if (m == 0) {
-        flush();
-        cur = -1;
-        for (++r; r < kRows; ++r) {
-          const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
-          if (z < 0 || z >= gz || y < 0 || y >= gy) continue;
-          m = masks[(size_t)r * N + i];
-          if (m) break;
+    // Row by row for all lanes together (mask and cell loads coalesced and
+    // issued at the same time), then the row's set bits in walk order; the
+    // cell partial sum is flushed into F when the cell changes.
+#pragma unroll 1
+    for (int r = 0; r < kRows; ++r) {
+      const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
+      if (z < 0 || z >= gz || y < 0 || y >= gy) continue;
+      unsigned long long m = masks[(size_t)r * N + i];
+      if (!m) continue;
+      const uint32_t row = d.c_off + (uint32_t)(z * (int)p.gridSize_yx + y * gx) + (uint32_t)x0;
+      const int nc = x1 - x0 + 1;
+      const uint32_t n0 = min(__ldg(count + row), maxpc);
+      const uint32_t n1 = nc > 1 ? min(__ldg(count + row + 1), maxpc) : 0u;
+      const uint32_t s0 = __ldg(start + row);
+      const uint32_t s1 = nc > 1 ? __ldg(start + row + 1) : 0u;
+      const uint32_t s2 = nc > 2 ? __ldg(start + row + 2) : 0u;
+      const uint32_t b1 = n0, b2 = n0 + n1;
+      int cur = -1;
+      while (m) {
+        const uint32_t b = (uint32_t)(__ffsll((long long)m) - 1);
+        m &= m - 1;
+        const int c = b >= b2 ? 2 : (b >= b1 ? 1 : 0);
+        if (c != cur) {
+          flush();
+          cur = c;
         }
-        if (r >= kRows) break;
-        const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
-        const uint32_t row = d.c_off + (uint32_t)(z * (int)p.gridSize_yx + y * gx) + (uint32_t)x0;
-        const int nc = x1 - x0 + 1;
-        const uint32_t n0 = min(__ldg(count + row), maxpc);
-        const uint32_t n1 = nc > 1 ? min(__ldg(count + row + 1), maxpc) : 0u;
-        s0 = __ldg(start + row);
-        s1 = nc > 1 ? __ldg(start + row + 1) : 0u;
-        s2 = nc > 2 ? __ldg(start + row + 2) : 0u;
-        b1 = n0;
-        b2 = n0 + n1;
+        const uint32_t j = c == 0 ? s0 + b : (c == 1 ? s1 + (b - b1) : s2 + (b - b2));
+        pair(j, cell);
       }
-      const uint32_t b = (uint32_t)(__ffsll((long long)m) - 1);
-      m &= m - 1;
-      const int c = b >= b2 ? 2 : (b >= b1 ? 1 : 0);
-      if (c != cur) {
-        flush();
-        cur = c;
-      }
-      const uint32_t j = c == 0 ? s0 + b : (c == 1 ? s1 + (b - b1) : s2 + (b - b2));
-      pair(j, cell);
+      flush();
     }
   } else {
 #pragma unroll 1
@@ -454,7 +473,7 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
                           p.gravity.z * p.gravity.z) + 1e-6f;
     const float s = __fmul_rn(p.particleMass, p.timeStep), isw = 1.f / (fa.sw + 1e-6f);
     float f[16];
-    f[0] = di / p.restDensity - 1.f;
+    f[0] = dens[i] / p.restDensity - 1.f;
     f[1] = pi / (p.restDensity * g * h);
     f[2] = fa.n * (1.f / 64.f);
     f[3] = fa.div * dt / h;
@@ -695,10 +714,12 @@ struct SphSystem {
   float4* vel[2] = {nullptr, nullptr};
   uint32_t* id[2] = {nullptr, nullptr};
   uint32_t *key = nullptr, *rank = nullptr, *slot = nullptr;
-  uint32_t *big_list = nullptr, *big_count = nullptr, *sort_scratch = nullptr;
-  unsigned big_blocks = 1;
+  uint32_t *big_list = nullptr, *sort_scratch = nullptr;
+  uint32_t *sort_list = nullptr, *sort_counters = nullptr;  // counters: list, big_list sizes
+  unsigned big_blocks = 1, sort_blocks = 1;
   uint32_t *count = nullptr, *start = nullptr, *scan_tmp = nullptr;
   float *dens = nullptr, *pres = nullptr;
+  float2* dp = nullptr;               // per particle: 1/density, pressure (force pass)
   unsigned long long* masks = nullptr;  // kRows x N neighbour masks (null: walks without)
   uint32_t* flags = nullptr;
   double* stats = nullptr;
@@ -768,25 +789,25 @@ template <bool kMask, int kThreads, int kMinBlocks, class Mark>
 void launch_walks_shape(SphSystem* s, cudaStream_t st, int b, int v, const StepOpts& o, Mark& mark) {
   const unsigned g = grid_for(s->N, kThreads);
   k_density<kMask, kThreads, kMinBlocks><<<g, kThreads, 0, st>>>(
-      o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->start, s->count, s->dens, s->pres,
+      o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->start, s->count, s->dens, s->pres, s->dp,
       s->masks, s->flags);
   mark();
   if (o.feat)
     k_force<kMask, kThreads, kMinBlocks, true><<<g, kThreads, 0, st>>>(
-        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->pres, s->start,
+        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->dp, s->start,
         s->count, s->masks, s->vel[v], o.fo);
   else
     k_force<kMask, kThreads, kMinBlocks, false><<<g, kThreads, 0, st>>>(
-        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->pres, s->start,
+        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->dp, s->start,
         s->count, s->masks, s->vel[v], o.fo);
 }
 
 template <bool kMask, class Mark>
 void launch_walks(SphSystem* s, cudaStream_t st, int b, int v, const StepOpts& o, Mark& mark) {
   switch (s->walk_shape) {
-    case 0: launch_walks_shape<kMask, 64, 8>(s, st, b, v, o, mark); break;
-    case 2: launch_walks_shape<kMask, 256, 2>(s, st, b, v, o, mark); break;
-    default: launch_walks_shape<kMask, 128, 4>(s, st, b, v, o, mark); break;
+    case 0: launch_walks_shape<kMask, 64, 16>(s, st, b, v, o, mark); break;
+    case 2: launch_walks_shape<kMask, 256, 4>(s, st, b, v, o, mark); break;
+    default: launch_walks_shape<kMask, 128, 8>(s, st, b, v, o, mark); break;
   }
 }
 
@@ -813,11 +834,13 @@ int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr,
   SPH_TRY(exclusive_scan(s->count, s->start, s->C, s->scan_tmp, st));
   mark();
   k_scatter_ids<<<gN, kBlock, 0, st>>>(s->N, s->key, s->rank, s->id[a], s->start, s->slot);
-  SPH_CUDA(cudaMemsetAsync(s->big_count, 0, sizeof(uint32_t), st), "step: clear big-cell count");
-  k_sort_cells<<<grid_for(s->C, kSortWarps), kSortWarps * 32, 0, st>>>(
-      s->C, s->start, s->count, s->slot, s->big_list, s->big_count);
+  SPH_CUDA(cudaMemsetAsync(s->sort_counters, 0, 2 * sizeof(uint32_t), st), "step: clear sort lists");
+  k_find_cells<<<grid_for(s->C, kBlock), kBlock, 0, st>>>(s->C, s->count, s->sort_list, s->sort_counters,
+                                                          s->big_list);
+  k_sort_cells<<<s->sort_blocks, kSortWarps * 32, 0, st>>>(s->start, s->count, s->slot,
+                                                           s->sort_list, s->sort_counters);
   k_sort_big_cells<<<s->big_blocks, kBigThreads, kBlockSortMax * sizeof(uint32_t), st>>>(
-      s->start, s->count, s->slot, s->big_list, s->big_count, s->sort_scratch);
+      s->start, s->count, s->slot, s->big_list, s->sort_counters + 1, s->sort_scratch);
   mark();
   k_place<<<gN, kBlock, 0, st>>>(sc, s->d_poff, s->S, s->N, s->pos[a], s->vel[v], s->id[a],
                                  s->key, s->start, s->count, s->slot, s->pos[b], s->vel[1 - v],
@@ -858,9 +881,9 @@ void free_all(SphSystem* s) {
   drop_graphs(s);
   void* bufs[] = {s->d_scenes, s->d_poff, s->d_coff, s->pos[0], s->pos[1], s->vel[0], s->vel[1],
                   s->id[0], s->id[1], s->key, s->rank, s->slot, s->count, s->start, s->scan_tmp,
-                  s->dens, s->pres, s->masks, s->flags, s->stats, s->staging, s->d_coarse,
+                  s->dens, s->pres, s->dp, s->masks, s->flags, s->stats, s->staging, s->d_coarse,
                   s->mlp_img, s->mlp_aux, s->feat, s->mlp_y, s->bk_vel, s->vstart, s->hist,
-                  s->big_list, s->big_count, s->sort_scratch};
+                  s->big_list, s->sort_counters, s->sort_list, s->sort_scratch};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
@@ -912,12 +935,14 @@ int create(const SimParams* scenes, uint32_t count, SphSystem** out) {
   ALLOC(s->rank, n, "cell ranks");
   ALLOC(s->slot, n, "cell slots");
   ALLOC(s->big_list, n / (kWarpSortMax + 1) + 1, "crowded-cell list");
-  ALLOC(s->big_count, 1, "crowded-cell count");
+  ALLOC(s->sort_list, n / (kLinearRank + 1) + 1, "cell sort list");
+  ALLOC(s->sort_counters, 2, "cell sort list sizes");
   ALLOC(s->sort_scratch, 2 * n, "cell sort scratch");
   ALLOC(s->count, c, "cell counts");
   ALLOC(s->start, c, "cell starts");
   ALLOC(s->scan_tmp, scan_scratch_words(c), "scan scratch");
   ALLOC(s->dens, n, "density");
+  ALLOC(s->dp, n, "inverse density and pressure");
   ALLOC(s->pres, n, "pressure");
   ALLOC(s->flags, 1, "flags");
   bool use_masks = SPH_WALK_MASKS != 0;
@@ -936,6 +961,7 @@ int create(const SimParams* scenes, uint32_t count, SphSystem** out) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     s->big_blocks = (unsigned)(sms > 0 ? sms : 1);
+    s->sort_blocks = (unsigned)(sms > 0 ? 8 * sms : 8);
   }
   if (rc == SPH_OK) {
     for (int k = 0; k < 2; ++k) {
