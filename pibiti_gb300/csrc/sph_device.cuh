@@ -270,23 +270,35 @@ __device__ __forceinline__ void force_pair(const ForceConsts& k, float4 xi, floa
   force_pair_near(k, vi, inv_di, pi, vj, inv_dj, pj, rx, ry, rz, dist2, acc);
 }
 
+// The pair term after the squared distance: returns whether r < h and then
+// sets f; the caller adds f to the cell's partial sum.
+__device__ __forceinline__ bool force_term(const ForceConsts& k, float4 vi, float inv_di, float pi,
+                                           float4 vj, float inv_dj, float pj, float rx, float ry,
+                                           float rz, float dist2, float3& f) {
+  const float dd = __fmul_rn(inv_di, inv_dj);
+  const float d12 = fminf(k.minDens, dd);
+  const float vx = __fsub_rn(vj.x, vi.x), vy = __fsub_rn(vj.y, vi.y), vz = __fsub_rn(vj.z, vi.z);
+  const float r = fmaxf(k.minDist, __fsqrt_rn(dist2));
+  const float c = __fsub_rn(k.h, r);
+  const float pterm = __fdiv_rn(__fmul_rn(__fmul_rn(c, k.spiky), __fadd_rn(pi, pj)), r);
+  const float s = __fmul_rn(c, d12);
+  f.x = __fmul_rn(__fmaf_rn(pterm, rx, __fmul_rn(k.vterm, vx)), s);
+  f.y = __fmul_rn(__fmaf_rn(pterm, ry, __fmul_rn(k.vterm, vy)), s);
+  f.z = __fmul_rn(__fmaf_rn(pterm, rz, __fmul_rn(k.vterm, vz)), s);
+  return r < k.h;
+}
+
 // The part of force_pair after the squared distance; the fused walk calls it
 // only for candidates not excluded by ForceConsts::h2_out (and for NaN).
 __device__ __forceinline__ void force_pair_near(const ForceConsts& k, float4 vi, float inv_di,
                                                 float pi, float4 vj, float inv_dj, float pj,
                                                 float rx, float ry, float rz, float dist2,
                                                 float3& acc) {
-  const float dd = __fmul_rn(inv_di, inv_dj);
-  const float d12 = fminf(k.minDens, dd);
-  const float vx = __fsub_rn(vj.x, vi.x), vy = __fsub_rn(vj.y, vi.y), vz = __fsub_rn(vj.z, vi.z);
-  const float r = fmaxf(k.minDist, __fsqrt_rn(dist2));
-  if (r < k.h) {
-    const float c = __fsub_rn(k.h, r);
-    const float pterm = __fdiv_rn(__fmul_rn(__fmul_rn(c, k.spiky), __fadd_rn(pi, pj)), r);
-    const float s = __fmul_rn(c, d12);
-    acc.x = __fadd_rn(acc.x, __fmul_rn(__fmaf_rn(pterm, rx, __fmul_rn(k.vterm, vx)), s));
-    acc.y = __fadd_rn(acc.y, __fmul_rn(__fmaf_rn(pterm, ry, __fmul_rn(k.vterm, vy)), s));
-    acc.z = __fadd_rn(acc.z, __fmul_rn(__fmaf_rn(pterm, rz, __fmul_rn(k.vterm, vz)), s));
+  float3 f;
+  if (force_term(k, vi, inv_di, pi, vj, inv_dj, pj, rx, ry, rz, dist2, f)) {
+    acc.x = __fadd_rn(acc.x, f.x);
+    acc.y = __fadd_rn(acc.y, f.y);
+    acc.z = __fadd_rn(acc.z, f.z);
   }
 }
 

@@ -380,6 +380,37 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   float3 F = make_float3(0.f, 0.f, 0.f);
   FeatAcc fa;
   const float inv_h = kFeat ? 1.f / p.h : 0.f;
+  auto feat = [&](float4 vj, float rx, float ry, float rz, float dist2) {
+    // network inputs (BF16): approximate reciprocals suffice
+    const float ir = rsqrtf(fmaxf(dist2, k.minDist * k.minDist));
+    const float r = fmaxf(k.minDist, dist2 * ir);
+    if (r < k.h) {
+      const float q = 1.f - r * inv_h, w = q * q;
+      const float dvx = vj.x - vi.x, dvy = vj.y - vi.y, dvz = vj.z - vi.z;
+      fa.sw += w;
+      fa.n += 1.f;
+      fa.div += w * (dvx * rx + dvy * ry + dvz * rz) * ir;
+      fa.rv[0] += w * dvx;
+      fa.rv[1] += w * dvy;
+      fa.rv[2] += w * dvz;
+      fa.rx[0] -= w * rx;
+      fa.rx[1] -= w * ry;
+      fa.rx[2] -= w * rz;
+    }
+  };
+  // Pair term of candidate j (the masks already hold dist2 < h2_out):
+  // returns whether r < h, with the term in f.
+  auto term = [&](uint32_t j, float3& f, bool with_feat) -> bool {
+    const float4 xj = __ldg(pos + j);
+    const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
+    const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
+    const float4 vj = __ldg(vel + j);
+    const float2 dpj = __ldg(dp + j);
+    const bool in = force_term(k, vi, inv_di, pi, vj, dpj.x, dpj.y, rx, ry, rz, dist2, f);
+    if (kFeat && with_feat) feat(vj, rx, ry, rz, dist2);
+    return in;
+  };
+  // Candidate j of the unmasked walk: skipped beyond h2_out before the loads.
   auto pair = [&](uint32_t j, float3& cell) {
     const float4 xj = __ldg(pos + j);
     const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
@@ -388,23 +419,7 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
       const float4 vj = __ldg(vel + j);
       const float2 dpj = __ldg(dp + j);
       force_pair_near(k, vi, inv_di, pi, vj, dpj.x, dpj.y, rx, ry, rz, dist2, cell);
-      if (kFeat) {  // network inputs (BF16): approximate reciprocals suffice
-        const float ir = rsqrtf(fmaxf(dist2, k.minDist * k.minDist));
-        const float r = fmaxf(k.minDist, dist2 * ir);
-        if (r < k.h) {
-          const float q = 1.f - r * inv_h, w = q * q;
-          const float dvx = vj.x - vi.x, dvy = vj.y - vi.y, dvz = vj.z - vi.z;
-          fa.sw += w;
-          fa.n += 1.f;
-          fa.div += w * (dvx * rx + dvy * ry + dvz * rz) * ir;
-          fa.rv[0] += w * dvx;
-          fa.rv[1] += w * dvy;
-          fa.rv[2] += w * dvz;
-          fa.rx[0] -= w * rx;
-          fa.rx[1] -= w * ry;
-          fa.rx[2] -= w * rz;
-        }
-      }
+      if (kFeat) feat(vj, rx, ry, rz, dist2);
     }
   };
   float3 cell = make_float3(0.f, 0.f, 0.f);
@@ -433,16 +448,42 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
       const uint32_t s2 = nc > 2 ? __ldg(start + row + 2) : 0u;
       const uint32_t b1 = n0, b2 = n0 + n1;
       int cur = -1;
+      auto cell_of_bit = [&](uint32_t b) { return b >= b2 ? 2 : (b >= b1 ? 1 : 0); };
+      auto index_of_bit = [&](uint32_t b, int c) {
+        return c == 0 ? s0 + b : (c == 1 ? s1 + (b - b1) : s2 + (b - b2));
+      };
+      // Two set bits per iteration: the two terms are independent (their
+      // loads, square roots and divisions overlap) and are added in order.
       while (m) {
-        const uint32_t b = (uint32_t)(__ffsll((long long)m) - 1);
+        const uint32_t ba = (uint32_t)(__ffsll((long long)m) - 1);
         m &= m - 1;
-        const int c = b >= b2 ? 2 : (b >= b1 ? 1 : 0);
-        if (c != cur) {
+        const bool two = m != 0;
+        const uint32_t bb = two ? (uint32_t)(__ffsll((long long)m) - 1) : ba;
+        m &= two ? m - 1 : m;
+        const int ca = cell_of_bit(ba), cb = cell_of_bit(bb);
+        float3 fa_, fb_;
+        const bool ina = term(index_of_bit(ba, ca), fa_, true);
+        const bool inb = term(index_of_bit(bb, cb), fb_, two);
+        if (ca != cur) {
           flush();
-          cur = c;
+          cur = ca;
         }
-        const uint32_t j = c == 0 ? s0 + b : (c == 1 ? s1 + (b - b1) : s2 + (b - b2));
-        pair(j, cell);
+        if (ina) {
+          cell.x = __fadd_rn(cell.x, fa_.x);
+          cell.y = __fadd_rn(cell.y, fa_.y);
+          cell.z = __fadd_rn(cell.z, fa_.z);
+        }
+        if (two) {
+          if (cb != cur) {
+            flush();
+            cur = cb;
+          }
+          if (inb) {
+            cell.x = __fadd_rn(cell.x, fb_.x);
+            cell.y = __fadd_rn(cell.y, fb_.y);
+            cell.z = __fadd_rn(cell.z, fb_.z);
+          }
+        }
       }
       flush();
     }
