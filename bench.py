@@ -38,7 +38,8 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s at 1M (plain vs learned, ≤1% density err); % HBM roofline"
 UNIT = "particle-steps/s"
 # Algorithmic bytes per particle (and per cell) each stage moves, every array
-# read or written once (the per-kernel model).
+# read or written once (intermediate arrays such as the neighbour masks are
+# not counted).
 STAGE_BYTES = {  # stage: (bytes per particle, bytes per cell)
     "integrate_count": (40, 12),
     "scan": (0, 8),
@@ -361,6 +362,32 @@ def workload_config(p, n=None):
     return cfg
 
 
+def run_state_tool(args) -> int:
+    """Saved states for profiling: a capture can then start at the crowded
+    phase of the workload after a handful of launches instead of thousands."""
+    import numpy as np
+    import torch
+    from pibiti_gb300 import configs
+    from pibiti_gb300.sph import ARRAY_POS, ARRAY_VEL, SPH, Scene
+    torch.cuda.set_device(0)
+    w = configs.dambreak_double()
+    p = Scene.parse(w.xml).params
+    with SPH(p) as s:
+        if args.save_state:
+            s.set_array(ARRAY_POS, w.pos)
+            s.set_array(ARRAY_VEL, w.vel)
+            s.update(args.warm_steps)
+            np.savez(args.save_state, pos=s.get_array(ARRAY_POS), vel=s.get_array(ARRAY_VEL))
+            print(json.dumps({"saved": args.save_state, "steps": args.warm_steps}))
+            return 0
+        z = np.load(args.stages)
+        s.set_array(ARRAY_POS, z["pos"])
+        s.set_array(ARRAY_VEL, z["vel"])
+        for _ in range(args.steps):
+            print(json.dumps({"stage_ms": s.step_timed()}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -373,10 +400,16 @@ def main():
                     help="ensemble: the 256-scene batched ensemble (a separate measurement)")
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-form measurement")
+    ap.add_argument("--save-state", metavar="NPZ",
+                    help="profiling aid: run --warm-steps steps of the workload, save the state, exit")
+    ap.add_argument("--stages", metavar="NPZ",
+                    help="profiling aid: load a saved state, print --steps per-stage step times")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.save_state or args.stages:
+        return run_state_tool(args)
     if args.workload == "ensemble":
         return run_ensemble(args)
 

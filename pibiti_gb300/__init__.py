@@ -1,1 +1,1 @@
-"""pibiti_gb300: a GB300-native SPH simulation step."""
+"""pibiti_gb300: a GB300-native SPH simulation step behind the reference's C ABI."""
