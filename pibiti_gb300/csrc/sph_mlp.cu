@@ -62,6 +62,18 @@ __device__ __forceinline__ void mma(float c[4], const uint32_t a[4], uint32_t b0
 
 __device__ __forceinline__ uint32_t ld32(const uint16_t* p) { return *reinterpret_cast<const uint32_t*>(p); }
 
+// The hardware tanh (one instruction, accurate to about 2^-11): its result
+// is rounded to BF16 (steps of 2^-9 relative) right after, so the
+// approximation changes an activation by at most one BF16 step.
+__device__ __forceinline__ float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ uint32_t tanh_pack2(float lo, float hi) {
+  return pack2(tanh_hw(lo), tanh_hw(hi));
+}
+
 // Packs the FP32 parameters into the BF16 kernel image.
 __global__ void k_pack(const float* __restrict__ prm, uint16_t* __restrict__ img) {
   uint16_t* w = img;
@@ -132,11 +144,11 @@ __device__ __forceinline__ void forward_tile(const uint16_t* sw, const float* sb
     mma(c, a, ld32(w), ld32(w + 8));
     const int kt = nt >> 1;
     if ((nt & 1) == 0) {
-      f.h1[kt][0] = pack2(tanhf(c[0]), tanhf(c[1]));
-      f.h1[kt][1] = pack2(tanhf(c[2]), tanhf(c[3]));
+      f.h1[kt][0] = tanh_pack2(c[0], c[1]);
+      f.h1[kt][1] = tanh_pack2(c[2], c[3]);
     } else {
-      f.h1[kt][2] = pack2(tanhf(c[0]), tanhf(c[1]));
-      f.h1[kt][3] = pack2(tanhf(c[2]), tanhf(c[3]));
+      f.h1[kt][2] = tanh_pack2(c[0], c[1]);
+      f.h1[kt][3] = tanh_pack2(c[2], c[3]);
     }
   }
   // layer 2: [16 x 64] x [64 x 64]
@@ -151,11 +163,11 @@ __device__ __forceinline__ void forward_tile(const uint16_t* sw, const float* sb
     }
     const int kt = nt >> 1;
     if ((nt & 1) == 0) {
-      f.h2[kt][0] = pack2(tanhf(c[0]), tanhf(c[1]));
-      f.h2[kt][1] = pack2(tanhf(c[2]), tanhf(c[3]));
+      f.h2[kt][0] = tanh_pack2(c[0], c[1]);
+      f.h2[kt][1] = tanh_pack2(c[2], c[3]);
     } else {
-      f.h2[kt][2] = pack2(tanhf(c[0]), tanhf(c[1]));
-      f.h2[kt][3] = pack2(tanhf(c[2]), tanhf(c[3]));
+      f.h2[kt][2] = tanh_pack2(c[0], c[1]);
+      f.h2[kt][3] = tanh_pack2(c[2], c[3]);
     }
   }
   // layer 3: [16 x 64] x [64 x 8]

@@ -3,8 +3,9 @@ NumPy oracle (oracle/mlp.py), which rounds to BF16 at the same places.
 
 Tolerances: outputs within 1e-2 of the output scale; each gradient block
 (W1, b1, W2, b2, W3, b3) within 2e-2 relative in the 2-norm; the loss within
-1e-3 relative.  The residual differences come from tanh (device vs double)
-occasionally flipping a BF16 rounding, and from FP32 accumulation order.
+1e-3 relative.  The residual differences come from tanh (the hardware
+approximation, accurate to about 2^-11, vs double) occasionally flipping a
+BF16 rounding, and from FP32 accumulation order.
 """
 import ctypes
 
