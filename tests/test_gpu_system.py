@@ -150,19 +150,11 @@ def test_grid_too_small_rejected(cuda):
     assert e.value.code == 3
 
 
-def test_million_particle_properties(cuda):
-    """The 1,048,576-particle double dam break: after 20 steps the neighbour
-    structures are a stable sort of (hash, original index), cell ranges
-    partition the particles, and density matches the double-precision
-    oracle on the GPU's own sorted positions."""
-    w = configs.dambreak_double(steps=20)
-    p = Scene.parse(w.xml).params
-    with system_from(p, w.pos, w.vel) as s:
-        s.update(20)
-        sh, cs, ce = s.cells()
-        dens, _ = s.fields()
-        pos = s.get_array(ARRAY_POS)
-    n = len(w.pos)
+def _check_structures(p, n, sh, cs, ce, dens, pos):
+    """Size-independent properties of one step's neighbour structures: a
+    stable sort of (hash, original index), cell ranges that partition the
+    particles, hashes of the sorted positions, density against the
+    double-precision oracle on the GPU's own sorted positions."""
     keys, ids = sh[:, 0].astype(np.int64), sh[:, 1].astype(np.int64)
     assert np.all(np.diff(keys) >= 0)
     same = np.diff(keys) == 0
@@ -173,12 +165,72 @@ def test_million_particle_properties(cuda):
     starts = np.concatenate([[0], np.cumsum(cnt)[:-1]])
     np.testing.assert_array_equal(cs[nz], starts[nz])
     np.testing.assert_array_equal(ce[nz], starts[nz] + cnt[nz])
-    # hashes are the hashes of the sorted positions
     spos = pos[ids]
     np.testing.assert_array_equal(oracle.calc_hash(p, spos)[:, 0], sh[:, 0])
     kv = np.stack([sh[:, 0], ids.astype(np.uint32)], axis=1)
     d64, _ = oracle.density(p, spos, kv, cs, fp64=True)
     np.testing.assert_allclose(dens, d64, rtol=DENS_RTOL, atol=1e-2)
+
+
+def test_million_particle_properties(cuda):
+    """The 1,048,576-particle double dam break after 20 steps."""
+    w = configs.dambreak_double(steps=20)
+    p = Scene.parse(w.xml).params
+    with system_from(p, w.pos, w.vel) as s:
+        s.update(20)
+        sh, cs, ce = s.cells()
+        dens, _ = s.fields()
+        pos = s.get_array(ARRAY_POS)
+    _check_structures(p, len(w.pos), sh, cs, ce, dens, pos)
+
+
+def test_stress_16m_properties(cuda):
+    """The stress configuration at full size: 16,777,216 particles uniform-
+    random in the lower 60% of a 4x1x4 box, h for ~40 neighbours (2.96 M
+    cells, 32-bit keys), after 3 steps with the grid rebuilt every step."""
+    w = configs.uniform_stress(steps=3)
+    p = Scene.parse(w.xml).params
+    assert p.numCells > 65536
+    with system_from(p, w.pos, w.vel) as s:
+        s.update(3)
+        sh, cs, ce = s.cells()
+        dens, _ = s.fields()
+        pos = s.get_array(ARRAY_POS)
+        st = s.stats()[0]
+    assert st[3] == 0  # nothing non-finite
+    _check_structures(p, len(w.pos), sh, cs, ce, dens, pos)
+
+
+def test_full_ensemble_scenes_match_separate_runs(cuda):
+    """The batched ensemble at full size (256 scenes, 4k-64k particles,
+    5.3 M in all): after 10 steps in one handle, every scene's structures
+    are a stable sort of (local hash, local index), and scenes 0, 127 and
+    255 equal separate
+    handles bit for bit (state and neighbour structures)."""
+    e = configs.ensemble()
+    ps = [Scene.parse(x).params for x in e.xmls]
+    with SPH(ps) as h:
+        h.set_array(ARRAY_POS, e.pos)
+        h.set_array(ARRAY_VEL, e.vel)
+        h.update(10)
+        epos, evel = h.get_array(ARRAY_POS), h.get_array(ARRAY_VEL)
+        offs = np.asarray(h.offsets, dtype=np.int64)
+        sh, _, _ = h.cells()
+    # hashes and original indices are local to each scene
+    keys, ids = sh[:, 0].astype(np.int64), sh[:, 1].astype(np.int64)
+    scene = np.repeat(np.arange(len(ps)), np.diff(offs))
+    inner = scene[1:] == scene[:-1]
+    dk = np.diff(keys)
+    assert np.all(dk[inner] >= 0)
+    assert np.all(np.diff(ids)[inner & (dk == 0)] > 0)
+    np.testing.assert_array_equal(np.sort(ids + offs[scene]), np.arange(len(e.pos)))
+    for k in (0, 127, 255):
+        a, b = offs[k], offs[k + 1]
+        with system_from(ps[k], e.pos[a:b], e.vel[a:b]) as s:
+            s.update(10)
+            np.testing.assert_array_equal(epos[a:b], s.get_array(ARRAY_POS))
+            np.testing.assert_array_equal(evel[a:b], s.get_array(ARRAY_VEL))
+            np.testing.assert_array_equal(sh[a:b], s.cells()[0])
 
 
 def test_walk_shapes_and_graph_lengths_agree(cuda):
