@@ -302,6 +302,43 @@ int sph_scene_default_index(const char* path, int* index);
 int sph_scene_reset(const SimParams* params, const SphSceneInfo* info, int type, uint64_t seed,
                     sph_float4* pos, sph_float4* vel, uint32_t* placed);
 
+/* Emitters, rain and Drop (App/Update.cpp:9-97, SPH_Init.cpp:83-117): the
+   reference computes the particles on the host and writes them with
+   setArray at a running emit index; here the functions below compute them
+   and the caller writes them with sph_set_array (the Python layer's
+   `emit` helper wraps the index as App::emitId does, splitting a write
+   that would run past the end, where the reference writes out of range). */
+#define SPH_NUM_EMIT 4
+typedef struct {
+  sph_float3 pos, rot; /* rot in degrees (x: pitch, y: yaw) */
+  float vel;
+  int32_t size, size2; /* size2 0: square */
+} SphEmitter;
+typedef struct {
+  SphEmitter emit[SPH_NUM_EMIT];
+  float rVel, r2Vel; /* rotor speeds (RotorVel, Rotor2Vel / WaveSpeed) */
+} SphSceneMotion;
+/* Emitters and rotor speeds of scene `index` of a file (Scene_Load.cpp:44-54,
+   98-105) / of one <Scene> element given as text. */
+int sph_scene_load_motion(const char* path, int index, SphSceneMotion* out);
+int sph_scene_parse_motion(const char* xml, SphSceneMotion* out);
+/* One frame of one emitter: size x size2 particles on a lattice of `spacing`
+   in the emitter's plane, rotated (glRotatef(rot.x, x) then glRotatef(-rot.y,
+   y), applied transposed), placed at pos, moving at vel along the rotated z
+   axis; pos.w = vel.w = 0.  Writes *count (0 when size is 0) particles; fails
+   when capacity is smaller. */
+int sph_emitter_particles(const SphEmitter* em, float spacing, sph_float4* pos, sph_float4* vel,
+                          uint32_t capacity, uint32_t* count);
+/* cSPH::Drop: a ball of radius dropR spacings at rest, centred in the box or
+   (random != 0) at a random place near the top drawn from a seeded
+   splitmix64 (the reference calls rand()); at most `capacity` particles. */
+int sph_drop_particles(const SimParams* params, const SphSceneInfo* info, int random,
+                       uint64_t seed, sph_float4* pos, sph_float4* vel, uint32_t capacity,
+                       uint32_t* count);
+/* The per-frame parameter updates of App::UpdateEmitter (Update.cpp:14-23):
+   rotor angles advanced by one time step, the dye-clear countdown. */
+int sph_scene_advance(SimParams* params, const SphSceneMotion* motion);
+
 #ifdef __cplusplus
 }
 #endif

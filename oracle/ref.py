@@ -54,6 +54,7 @@ def lib() -> ctypes.CDLL:
         L.ref_scene_count.argtypes = [ctypes.c_char_p]
         L.ref_scene_load.argtypes = [ctypes.c_char_p, ctypes.c_int, vp, vp]
         L.ref_scene_default.argtypes = [vp, vp]
+        L.ref_scene_motion.argtypes = [ctypes.c_char_p, ctypes.c_int, vp]
         _lib = L
     return _lib
 
@@ -152,6 +153,15 @@ def scene_load(path: str, index: int):
     if rc != 0:
         raise ValueError(f"reference scene loader failed rc={rc}")
     return SimParams.from_bytes(buf.raw), list(extra)[:13]
+
+
+def scene_motion(path: str, index: int) -> np.ndarray:
+    """Emitters (4 x [pos3, rot3, vel, size, size2]) and rVel, r2Vel."""
+    out = (ctypes.c_float * 38)()
+    rc = lib().ref_scene_motion(path.encode(), index, out)
+    if rc != 0:
+        raise ValueError(f"reference scene loader failed rc={rc}")
+    return np.array(list(out), np.float32)
 
 
 def scene_default():

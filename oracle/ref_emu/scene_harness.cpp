@@ -59,6 +59,32 @@ int ref_scene_load(const char* path, int index, SimParams* out, float* extra) {
   return 0;
 }
 
+/* Emitters and rotor speeds of scene `index`: per emitter pos[3], rot[3],
+   vel, size, size2 (9 floats, NumEmit emitters), then rVel, r2Vel. */
+int ref_scene_motion(const char* path, int index, float* out) {
+  TiXmlDocument doc;
+  if (!doc.LoadFile(path)) return -1;
+  TiXmlElement* s = nth_scene(doc, index);
+  if (!s) return -2;
+  Scene sc(s);
+  for (int e = 0; e < NumEmit; ++e) {
+    const Emitter& em = sc.emit[e];
+    float* o = out + 9 * e;
+    o[0] = em.pos.x;
+    o[1] = em.pos.y;
+    o[2] = em.pos.z;
+    o[3] = em.rot.x;
+    o[4] = em.rot.y;
+    o[5] = em.rot.z;
+    o[6] = em.vel;
+    o[7] = (float)em.size;
+    o[8] = (float)em.size2;
+  }
+  out[9 * NumEmit] = sc.rVel;
+  out[9 * NumEmit + 1] = sc.r2Vel;
+  return 0;
+}
+
 /* Scene() (Scene.h:56): defaults plus derivations, no XML. */
 int ref_scene_default(SimParams* out, float* extra) {
   Scene sc;

@@ -35,6 +35,19 @@ class SceneInfo(ctypes.Structure):
                 ("rain", ctypes.c_int32)]
 
 
+NUM_EMIT = 4
+
+
+class Emitter(ctypes.Structure):
+    from .params import Float3 as _F3
+    _fields_ = [("pos", _F3), ("rot", _F3), ("vel", ctypes.c_float), ("size", ctypes.c_int32),
+                ("size2", ctypes.c_int32)]
+
+
+class SceneMotion(ctypes.Structure):
+    _fields_ = [("emit", Emitter * NUM_EMIT), ("rVel", ctypes.c_float), ("r2Vel", ctypes.c_float)]
+
+
 _lib = None
 vp = ctypes.c_void_p
 u32 = ctypes.c_uint32
@@ -84,6 +97,11 @@ SIGNATURES = {
     "sph_scene_default": [P(SimParams), P(SceneInfo)],
     "sph_scene_default_index": [ctypes.c_char_p, P(i32)],
     "sph_scene_reset": [P(SimParams), P(SceneInfo), i32, ctypes.c_uint64, vp, vp, P(u32)],
+    "sph_scene_load_motion": [ctypes.c_char_p, i32, P(SceneMotion)],
+    "sph_scene_parse_motion": [ctypes.c_char_p, P(SceneMotion)],
+    "sph_emitter_particles": [P(Emitter), ctypes.c_float, vp, vp, u32, P(u32)],
+    "sph_drop_particles": [P(SimParams), P(SceneInfo), i32, ctypes.c_uint64, vp, vp, u32, P(u32)],
+    "sph_scene_advance": [P(SimParams), P(SceneMotion)],
     "sph_mlp_param_count": [],
     "sph_mlp_packed_bytes": [],
     "sph_mlp_pack": [vp, vp, vp],

@@ -245,6 +245,7 @@ struct SceneState {
   SimParams p;
   SphSceneInfo info;
   float rVel, r2Vel;
+  SphEmitter emit[SPH_NUM_EMIT];
 };
 
 // Scene::InitDefault (Scene.cpp:7-66)
@@ -312,6 +313,7 @@ void init_default(SceneState& s) {
   p.r2twist = 1;
   s.rVel = 0;
   s.r2Vel = 1;
+  for (SphEmitter& em : s.emit) em.vel = 1.5f;  // Emitter() (Scene.h:13)
   snprintf(s.info.title, sizeof(s.info.title), "No name");
   s.info.chapter = 0;
   for (int i = 0; i < SPH_NUM_ACC; ++i) {
@@ -364,6 +366,25 @@ void from_xml(SceneState& s, const XmlElem& e) {
   A("chapter") in.chapter = 1;
   AF("dropR", in.dropR);
   AI("rain", in.rain);
+  // emitters (Scene_Load.cpp:44-54): the first in attributes, up to
+  // SPH_NUM_EMIT as <Emitter> children (which start again at index 0)
+  AI("EmitSize", s.emit[0].size);
+  AV("EmitPos", s.emit[0].pos);
+  AF("EmitVel", s.emit[0].vel);
+  AI("EmitSize2", s.emit[0].size2);
+  AV("EmitRot", s.emit[0].rot);
+  {
+    int ie = 0;
+    for (const auto& k : e.kids) {
+      if (k->name != "Emitter" || ie >= SPH_NUM_EMIT) continue;
+      SphEmitter& em = s.emit[ie++];
+      if ((a = k->attr("size"))) em.size = to_int(a);
+      if ((a = k->attr("pos"))) em.pos = to_vec3(a);
+      if ((a = k->attr("vel"))) em.vel = to_float(a);
+      if ((a = k->attr("size2"))) em.size2 = to_int(a);
+      if ((a = k->attr("rot"))) em.rot = to_vec3(a);
+    }
+  }
   // accelerators as children (max NumAcc)
   int i = 0;
   for (const auto& k : e.kids) {
@@ -496,6 +517,24 @@ void update(SceneState& s) {
 void finish(const SceneState& s, SimParams* out, SphSceneInfo* info) {
   *out = s.p;
   if (info) *info = s.info;
+}
+
+void motion_of(const SceneState& s, SphSceneMotion* m) {
+  memset(m, 0, sizeof(*m));
+  for (int k = 0; k < SPH_NUM_EMIT; ++k) m->emit[k] = s.emit[k];
+  m->rVel = s.rVel;
+  m->r2Vel = s.r2Vel;
+}
+
+int scene_element(const std::string& xml, std::unique_ptr<XmlElem>* root, const XmlElem** e) {
+  SPH_TRY(parse_doc(xml, root));
+  *e = root->get();
+  if ((*e)->name != "Scene") {
+    const auto sc = scenes_of(**root);
+    if (sc.empty()) return fail(SPH_ERR_XML, "no <Scene> element");
+    *e = sc[0];
+  }
+  return SPH_OK;
 }
 
 // rand()/RAND_MAX stand-in for cSPH::Reset's random fill: splitmix64.
@@ -679,6 +718,129 @@ int sph_scene_reset(const SimParams* params, const SphSceneInfo* info, int type,
   }
   if (placed) *placed = i;
   if (i < N) return fail(SPH_ERR_PARAMS, "scene_reset: init volume accepted only %u of %u particles", i, N);
+  return SPH_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int sph_scene_load_motion(const char* path, int index, SphSceneMotion* out) {
+  if (!path || !out) return fail(SPH_ERR_ARG, "scene_load_motion: null argument");
+  std::string text;
+  SPH_TRY(read_file(path, &text));
+  std::unique_ptr<XmlElem> root;
+  SPH_TRY(parse_doc(text, &root));
+  const auto sc = scenes_of(*root);
+  if (index < 0 || index >= (int)sc.size())
+    return fail(SPH_ERR_ARG, "scene index %d out of range (%zu scenes)", index, sc.size());
+  SceneState s;
+  init_default(s);
+  from_xml(s, *sc[index]);
+  motion_of(s, out);
+  return SPH_OK;
+}
+
+int sph_scene_parse_motion(const char* xml, SphSceneMotion* out) {
+  if (!xml || !out) return fail(SPH_ERR_ARG, "scene_parse_motion: null argument");
+  std::unique_ptr<XmlElem> root;
+  const XmlElem* e = nullptr;
+  SPH_TRY(scene_element(std::string(xml), &root, &e));
+  SceneState s;
+  init_default(s);
+  from_xml(s, *e);
+  motion_of(s, out);
+  return SPH_OK;
+}
+
+// App::UpdateEmitter, emitter part (App/Update.cpp:64-91).  The rotation
+// is the modelview matrix M = Rx(rot.x) Ry(-rot.y) (glRotatef in degrees)
+// applied transposed (App::mulTr, Input.cpp:587-592): r = M^T v.
+int sph_emitter_particles(const SphEmitter* em, float spacing, sph_float4* pos, sph_float4* vel,
+                          uint32_t capacity, uint32_t* count) {
+  if (!em || !count) return fail(SPH_ERR_ARG, "emitter_particles: null argument");
+  *count = 0;
+  if (em->size <= 0) return SPH_OK;
+  const int ex = em->size, ey = em->size2 == 0 ? ex : em->size2;
+  const uint32_t n = (uint32_t)ex * (uint32_t)ey;
+  if (n > capacity || !pos || !vel) return fail(SPH_ERR_ARG, "emitter_particles: room for %u particles needed", n);
+  const float deg = 3.14159265358979f / 180.f;
+  const float ca = cosf(em->rot.x * deg), sa = sinf(em->rot.x * deg);
+  const float cb = cosf(-em->rot.y * deg), sb = sinf(-em->rot.y * deg);
+  // M = Rx(a) Ry(b), row-major m[r][c]
+  const float m[3][3] = {{cb, 0.f, sb}, {sa * sb, ca, -sa * cb}, {-ca * sb, sa, ca * cb}};
+  auto mul_tr = [&](float x, float y, float z, float* r) {
+    for (int c = 0; c < 3; ++c) r[c] = x * m[0][c] + y * m[1][c] + z * m[2][c];
+  };
+  float v3[3];
+  mul_tr(0.f, 0.f, em->vel, v3);
+  const float zx = (float)(ex - 1) * 0.5f, zy = (float)(ey - 1) * 0.5f;
+  uint32_t i = 0;
+  for (int y = 0; y < ey; ++y)
+    for (int x = 0; x < ex; ++x, ++i) {
+      float r[3];
+      mul_tr(((float)x - zx) * spacing, ((float)y - zy) * spacing, -spacing, r);
+      pos[i] = {r[0] + em->pos.x, r[1] + em->pos.y, r[2] + em->pos.z, 0.f};
+      vel[i] = {v3[0], v3[1], v3[2], 0.f};
+    }
+  *count = n;
+  return SPH_OK;
+}
+
+// cSPH::Drop (SPH_Init.cpp:83-117): a ball of particles of radius dropR
+// spacings, at the box centre, or (random) at a random place near the top;
+// at most `capacity` particles (the reference stops at numParticles).
+int sph_drop_particles(const SimParams* params, const SphSceneInfo* info, int random,
+                       uint64_t seed, sph_float4* pos, sph_float4* vel, uint32_t capacity,
+                       uint32_t* count) {
+  if (!params || !info || !count) return fail(SPH_ERR_ARG, "drop_particles: null argument");
+  const SimParams& p = *params;
+  const float r = info->dropR, spc = info->spacing, r2 = r * r, db = (r + 1.f) * spc, d = 0.5f;
+  sph_float3 c = f3(0.5f, 0.5f, 0.5f);
+  if (random) {
+    Rng g{seed};
+    const uint32_t t = p.bndType;
+    c.y = (t == SPH_BND_BOX || t == SPH_BND_CYL_Y) ? 1.0f : 0.75f;
+    if (t == SPH_BND_BOX || t == SPH_BND_CYL_Z) {
+      c.x = g.next();
+      c.z = g.next();
+    } else {
+      const float rr = g.next(), k = g.next() * 2.f * 3.14159265358979f;
+      c.x = d + d * cosf(k) * rr;
+      c.z = d - d * sinf(k) * rr;
+    }
+  }
+  const sph_float3 ws = p.worldSizeD;
+  const sph_float3 posw = f3(p.worldMinD.x + db + c.x * (ws.x - 2.f * db),
+                             p.worldMinD.y + db + c.y * (ws.y - 2.f * db),
+                             p.worldMinD.z + db + c.z * (ws.z - 2.f * db));
+  const int ir = (int)-r;  // the reference's int loop bound from -r
+  uint32_t n = 0;
+  for (int z = ir; z <= r; ++z)
+    for (int y = ir; y <= r; ++y)
+      for (int x = ir; x <= r; ++x)
+        if ((float)(x * x + y * y + z * z) <= r2 && n < capacity) {  // "a < numParticles"
+          if (!pos || !vel) return fail(SPH_ERR_ARG, "drop_particles: null output");
+          pos[n] = {x * spc + posw.x, y * spc + posw.y, z * spc + posw.z, 1.f};
+          vel[n] = {0.f, 0.f, 0.f, 0.f};
+          ++n;
+        }
+  *count = n;
+  return SPH_OK;
+}
+
+// The per-frame parameter updates of App::UpdateEmitter (App/Update.cpp:
+// 14-23): rotor angles and the dye-clear countdown.
+int sph_scene_advance(SimParams* p, const SphSceneMotion* m) {
+  if (!p || !m) return fail(SPH_ERR_ARG, "scene_advance: null argument");
+  if (m->rVel != 0.f) {
+    p->rAngle += m->rVel * p->timeStep;
+    if (p->r2Dist > 0.f) {
+      p->r2Angle += m->rVel * m->r2Vel * p->timeStep;
+      p->r2twist = m->r2Vel < 0.f ? -1.f : 1.f;
+    }
+  }
+  if (p->dyeClear > 0) p->dyeClear--;
   return SPH_OK;
 }
 

@@ -16,7 +16,7 @@ from typing import Iterable, Optional, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import ARRAY_POS, ARRAY_VEL, SceneInfo, check, lib
+from ._lib import ARRAY_POS, ARRAY_VEL, SceneInfo, SceneMotion, check, lib
 from .params import SimParams
 
 __all__ = ["Scene", "SPH", "ARRAY_POS", "ARRAY_VEL", "stage"]
@@ -41,9 +41,10 @@ def _buf(x, dtype=np.float32, cols=4):
 class Scene:
     """One scene: SimParams plus the init data Scene keeps beside it."""
 
-    def __init__(self, params: SimParams, info: SceneInfo):
+    def __init__(self, params: SimParams, info: SceneInfo, motion: Optional[SceneMotion] = None):
         self.params = params
         self.info = info
+        self.motion = motion if motion is not None else SceneMotion()
 
     @property
     def title(self) -> str:
@@ -57,15 +58,17 @@ class Scene:
 
     @classmethod
     def parse(cls, xml: str) -> "Scene":
-        p, i = SimParams(), SceneInfo()
+        p, i, m = SimParams(), SceneInfo(), SceneMotion()
         check(lib().sph_scene_parse(xml.encode(), ctypes.byref(p), ctypes.byref(i)))
-        return cls(p, i)
+        check(lib().sph_scene_parse_motion(xml.encode(), ctypes.byref(m)))
+        return cls(p, i, m)
 
     @classmethod
     def load(cls, path: str, index: int) -> "Scene":
-        p, i = SimParams(), SceneInfo()
+        p, i, m = SimParams(), SceneInfo(), SceneMotion()
         check(lib().sph_scene_load(path.encode(), index, ctypes.byref(p), ctypes.byref(i)))
-        return cls(p, i)
+        check(lib().sph_scene_load_motion(path.encode(), index, ctypes.byref(m)))
+        return cls(p, i, m)
 
     @staticmethod
     def count(path: str) -> int:
@@ -94,6 +97,36 @@ class Scene:
                                     ctypes.c_void_p(pos.ctypes.data),
                                     ctypes.c_void_p(vel.ctypes.data), ctypes.byref(placed)))
         return pos, vel
+
+    def emitter_particles(self, k: int):
+        """Particles emitter k writes in one frame (App/Update.cpp:64-91):
+        (pos, vel) float32 (n, 4); empty when the emitter is off."""
+        em = self.motion.emit[k]
+        n = max(em.size, 0) * (em.size2 if em.size2 else max(em.size, 0))
+        pos = np.zeros((max(n, 1), 4), np.float32)
+        vel = np.zeros((max(n, 1), 4), np.float32)
+        cnt = ctypes.c_uint32()
+        check(lib().sph_emitter_particles(ctypes.byref(em), self.info.spacing,
+                                          ctypes.c_void_p(pos.ctypes.data),
+                                          ctypes.c_void_p(vel.ctypes.data), len(pos),
+                                          ctypes.byref(cnt)))
+        return pos[:cnt.value], vel[:cnt.value]
+
+    def drop_particles(self, random: bool = False, seed: int = 1, capacity: Optional[int] = None):
+        """cSPH::Drop (SPH_Init.cpp:83-117): (pos, vel) of the dropped ball."""
+        r = int(self.info.dropR) + 1
+        cap = (2 * r + 1) ** 3 if capacity is None else capacity
+        pos = np.zeros((max(cap, 1), 4), np.float32)
+        vel = np.zeros((max(cap, 1), 4), np.float32)
+        cnt = ctypes.c_uint32()
+        check(lib().sph_drop_particles(ctypes.byref(self.params), ctypes.byref(self.info),
+                                       int(random), seed, ctypes.c_void_p(pos.ctypes.data),
+                                       ctypes.c_void_p(vel.ctypes.data), cap, ctypes.byref(cnt)))
+        return pos[:cnt.value], vel[:cnt.value]
+
+    def advance(self) -> None:
+        """One frame of the parameter updates (rotor angles, dye clear)."""
+        check(lib().sph_scene_advance(ctypes.byref(self.params), ctypes.byref(self.motion)))
 
 
 class SPH:
@@ -162,6 +195,25 @@ class SPH:
         ptr, dev, keep = _buf(out)
         check(lib().sph_get_array(self._h, which, ptr, int(dev)))
         return out
+
+    def emit(self, pos, vel, emit_id: int) -> int:
+        """Writes emitted particles at the running emit index (App::emitId,
+        App/Update.cpp:87-90) with setArray and returns the next index.  A
+        block that would run past the last particle continues at 0 (the
+        reference writes past the end of its buffers there)."""
+        n, total = len(pos), self.n
+        if n == 0:
+            return emit_id
+        if n > total or not 0 <= emit_id < total:
+            raise ValueError("emit: block larger than the system or index out of range")
+        first = min(n, total - emit_id)
+        self.set_array(ARRAY_POS, np.ascontiguousarray(pos[:first]), start=emit_id)
+        self.set_array(ARRAY_VEL, np.ascontiguousarray(vel[:first]), start=emit_id)
+        if first < n:
+            self.set_array(ARRAY_POS, np.ascontiguousarray(pos[first:]), start=0)
+            self.set_array(ARRAY_VEL, np.ascontiguousarray(vel[first:]), start=0)
+        nxt = emit_id + n
+        return nxt - total if nxt >= total else nxt
 
     def update(self, steps: int = 1) -> None:
         """cSPH::Update (SPH_Update.cpp:12-81), `steps` times."""

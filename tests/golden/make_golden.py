@@ -55,6 +55,10 @@ EXTRA_SCENES = [
     '<Scene PumpAngOut="0.3" PumpHClose="-0.02" PumpRadIn="0.5" ExitVel="0.05" ExitDist="0.03" '
     's1="0.8" s2="0.85" s3="1.1" s4="0.7" s5="0.9" s6="0.8" RotorSizes="1 5 10" RotorType="0" '
     'Rotor2Dist="0.1" colParR="2.5" colParSpc="0.6" RotorBlades="3" />',
+    '<Scene EmitSize="4" EmitPos="0.1 0.2 -0.1" EmitVel="2.5" EmitSize2="3" EmitRot="30 -45" '
+    'RotorVel="1.5" Rotor2Vel="-0.5" dropR="3.5" rain="20" spacing="1.2" />',
+    '<Scene EmitSize="5" EmitPos="0.3 0.3 0.3"><Emitter size="3" pos="0 0.1 0" vel="1" rot="10 20" />'
+    '<Emitter size="2" size2="6" pos="-0.2 0 0.1" rot="-90 180" /></Scene>',
 ]
 
 
@@ -72,20 +76,33 @@ def ref_scene_from_xml(xml: str):
         os.unlink(path)
 
 
+def ref_motion_from_xml(xml: str):
+    with tempfile.NamedTemporaryFile("w", suffix=".xml", delete=False) as f:
+        f.write("<SPH>" + xml + "</SPH>")
+        path = f.name
+    try:
+        return ref.scene_motion(path, 0)
+    finally:
+        os.unlink(path)
+
+
 def make_scenes():
     xmls = list(EXTRA_SCENES)
     xmls += [configs.dambreak_small(side=16).xml, configs.dambreak_small(side=32).xml,
              configs.dambreak_double().xml]
-    params, extras = [], []
+    params, extras, motion = [], [], []
     for x in xmls:
         p, ex = ref_scene_from_xml(x)
         params.append(_param_bytes(p))
         extras.append(np.array(ex, np.float32))
+        motion.append(ref_motion_from_xml(x))
     n = ref.scene_count(SCENES_XML)
     file_params = np.stack([_param_bytes(ref.scene_load(SCENES_XML, i)[0]) for i in range(n)])
     file_extras = np.stack([np.array(ref.scene_load(SCENES_XML, i)[1], np.float32) for i in range(n)])
+    file_motion = np.stack([ref.scene_motion(SCENES_XML, i) for i in range(n)])
     np.savez_compressed(os.path.join(OUT, "scenes.npz"), xml=np.array(xmls), params=np.stack(params),
-                        extras=np.stack(extras), file_params=file_params, file_extras=file_extras)
+                        extras=np.stack(extras), motion=np.stack(motion), file_params=file_params,
+                        file_extras=file_extras, file_motion=file_motion)
     print(f"scenes.npz: {len(xmls)} scene elements, {n} scenes of Scenes.xml")
 
 
