@@ -30,7 +30,7 @@ def test_emit_wraps_and_steps(cuda):
         dp, dv = base.drop_particles(capacity=s.n - nxt)
         nxt2 = s.emit(dp, dv, nxt)
         np.testing.assert_array_equal(s.get_array(ARRAY_POS)[nxt:nxt + len(dp)], dp)
-        assert nxt2 == nxt + len(dp)
+        assert nxt2 == (nxt + len(dp)) % s.n
         s.update(5)
         st = s.stats()[0]
         assert st[3] == 0 and np.isfinite(s.get_array(ARRAY_POS)).all()
