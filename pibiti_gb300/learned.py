@@ -10,7 +10,9 @@ units of |g| dt_coarse.
 
 Training data comes from the batched ensemble (configs.ensemble): from a state
 of the fine-dt run, one featured coarse step and SUBSTEPS fine steps give one
-(features, target) pair per particle.  Training runs the project's own
+(features, target) pair per particle.  Then, for a few rounds, the states the
+learned integrator itself visits are labelled the same way and added (the
+network then learns to correct the states its own errors lead to).  Training runs the project's own
 forward/backward kernels (sph_mlp_train_pass) with Adam (sph_mlp_adam).
 Device buffers are torch tensors passed by pointer.
 """
@@ -133,6 +135,50 @@ def generate(xmls, pos, vel, sizes, snapshots: int = 8, warm: int = 20, gap: int
 # steps, steps between snapshots) of the fine run; the first covers the
 # early collapse of each dam break, the second the rest of 2000 steps.
 PHASES = ((6, 20, 30), (9, 220, 200))
+
+
+def generate_rollout(model: "Model", xmls, pos, vel, sizes, snapshots: int = 8, warm: int = 20,
+                     gap: int = 60, substeps: int = SUBSTEPS, drift: float = -1.0):
+    """Like generate(), but from the states the learned integrator itself
+    visits: the scenes advance with learned_step (`gap` coarse steps between
+    snapshots, no density check), and each snapshot is labelled with one
+    featured coarse step and `substeps` fine steps from that state."""
+    import torch
+    ps = [Scene.parse(x).params for x in xmls]
+    lrn, fine, coarse = SPH(ps), SPH(ps), SPH(ps)
+    lrn.set_array(ARRAY_POS, pos)
+    lrn.set_array(ARRAY_VEL, vel)
+    lrn.update(warm)
+    model.install(lrn)
+    set_options(lrn, drift)
+    n = lrn.n
+    gdt = _g_dt(ps, sizes, substeps, torch)
+    tp = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    tv = torch.empty_like(tp)
+    vc = torch.empty_like(tp)
+    vf = torch.empty_like(tp)
+    feats, targets = [], []
+    for _ in range(snapshots):
+        learned_step(lrn, gap, substeps, 1e9)
+        lrn.get_array(ARRAY_POS, tp)
+        lrn.get_array(ARRAY_VEL, tv)
+        torch.cuda.synchronize()
+        for h in (coarse, fine):
+            h.set_array(ARRAY_POS, tp)
+            h.set_array(ARRAY_VEL, tv)
+        f = torch.empty((n, 16), dtype=torch.float32, device="cuda")
+        ids = torch.empty(n, dtype=torch.int32, device="cuda")
+        features_step(coarse, f, ids, substeps)
+        coarse.get_array(ARRAY_VEL, vc)
+        fine.update(substeps)
+        fine.get_array(ARRAY_VEL, vf)
+        torch.cuda.synchronize()
+        t = (vf - vc)[:, :3] / gdt[:, None]
+        feats.append(f)
+        targets.append(t[ids.long()].contiguous())
+    for h in (lrn, fine, coarse):
+        h.close()
+    return torch.cat(feats), torch.cat(targets)
 
 
 def generate_phases(xmls, pos, vel, sizes, phases=PHASES, substeps: int = SUBSTEPS):
@@ -319,6 +365,8 @@ def main(argv=None) -> int:
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--epochs", type=int, default=16)
     ap.add_argument("--batch", type=int, default=32768)
+    ap.add_argument("--rounds", type=int, default=2,
+                    help="rounds of training on the learned integrator's own states")
     ap.add_argument("--fine-steps", type=int, default=2000)
     ap.add_argument("--model", default=MODEL_PATH)
     a = ap.parse_args(argv)
@@ -331,8 +379,19 @@ def main(argv=None) -> int:
         log(f"generated {f.shape[0]} samples in {time.perf_counter() - t0:.1f} s")
         t0 = time.perf_counter()
         model = train(f, t, epochs=a.epochs, batch=a.batch, log=log)
+        feats, targets = [f], [t]
+        for rnd in range(a.rounds):
+            # the states the current model's integrator visits, labelled by fine steps
+            fr, tr = generate_rollout(model, e.xmls, e.pos, e.vel, e.sizes, snapshots=10, warm=20,
+                                      gap=50)
+            feats.append(fr)
+            targets.append(tr)
+            log(f"round {rnd + 1}: {sum(x.shape[0] for x in feats)} samples")
+            model = train(torch.cat(feats), torch.cat(targets), epochs=a.epochs, batch=a.batch,
+                          log=log)
         model.info.update({"scenes": a.scenes, "phases": PHASES, "epochs": a.epochs,
-                           "batch": a.batch, "train_s": time.perf_counter() - t0})
+                           "batch": a.batch, "rounds": a.rounds,
+                           "train_s": time.perf_counter() - t0})
         model.save(a.model)
         w = configs.dambreak_small(side=32, seed=9)
         print(json.dumps({"trained": model.info,
