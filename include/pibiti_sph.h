@@ -164,6 +164,19 @@ int sph_step(SphSystem* sys, uint32_t steps);
    directly, so a whole run of steps_per_graph steps is one launch. */
 int sph_set_graph_steps(SphSystem* sys, uint32_t steps_per_graph);
 
+/* Colour and dye from every following step, the output of the reference's
+   collide() (vboClr, dDyeColor; System.cu:405-546): clr gets one float4
+   per particle and dye one float per particle, both device buffers of
+   sph_num_particles records in original order owned by the caller (the dye
+   is read and written: it carries over from step to step, as in the
+   reference).  The colour type and constants are SimParams' (clrType,
+   brightness, contrast, iHue, dye*).  NULL clr turns the output off; dye
+   may be NULL.  The step's velocity increment is taken as v_new - v_old,
+   and the CLR_Vel foam sum skips neighbour cells beyond the grid edge
+   (the reference wraps there); sph_collide keeps the reference's exact
+   form of both. */
+int sph_set_color_output(SphSystem* sys, sph_float4* clr, float* dye);
+
 /* Launch shape of the density and force walks: 0 = 64 threads per block,
    1 = 128 (default), 2 = 256, each compiled for full occupancy at that size. */
 int sph_set_walk_shape(SphSystem* sys, uint32_t shape);

@@ -617,6 +617,48 @@ __global__ void k_apply_correction(const SceneDesc* __restrict__ sc, const uint3
   }
 }
 
+// Colour and dye of the step (computeForceD's colour part, System.cu:405-546)
+// for a caller that asked for them, after the force pass: clr and dye are
+// in original order (the dye is read and written: it carries over between
+// steps).  The velocity increment is taken as v_new - v_start; the CLR_Vel
+// foam sum walks the in-grid neighbour cells in the reference's x-outer
+// order over the same truncated cell contents (the reference also visits
+// the wrapped cells beyond the grid edge, which the fused step skips).
+__global__ void k_color(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S,
+                        uint32_t N, const float4* __restrict__ pos,
+                        const float4* __restrict__ vel_start, const float4* __restrict__ vel_new,
+                        const float* __restrict__ dens, const uint32_t* __restrict__ start,
+                        const uint32_t* __restrict__ count, const uint32_t* __restrict__ id,
+                        float4* __restrict__ clr, float* __restrict__ dye) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
+  const SimParams& p = d.p;
+  const float4 xi = pos[i], vi = vel_start[i], vn = vel_new[i];
+  const float3 add = make_float3(__fsub_rn(vn.x, vi.x), __fsub_rn(vn.y, vi.y), __fsub_rn(vn.z, vi.z));
+  float vdiff = 0.f;
+  if (p.clrType == SPH_CLR_VEL) {
+    const int3 g = grid_pos(p, xi);
+    const int gx = (int)p.gridSize.x, gy = (int)p.gridSize.y, gz = (int)p.gridSize.z;
+    const int cx = min(max(g.x, 0), gx - 1), cy = min(max(g.y, 0), gy - 1), cz = min(max(g.z, 0), gz - 1);
+    for (int x = -1; x < 2; ++x)
+      for (int y = -1; y < 2; ++y)
+        for (int z = -1; z < 2; ++z) {
+          const int ux = cx + x, uy = cy + y, uz = cz + z;
+          if (ux < 0 || ux >= gx || uy < 0 || uy >= gy || uz < 0 || uz >= gz) continue;
+          const uint32_t c = d.c_off + (uint32_t)(uz * (int)p.gridSize_yx + uy * gx + ux);
+          const uint32_t n = min(__ldg(count + c), p.maxParInCell), s0 = __ldg(start + c);
+          for (uint32_t q = 0; q < n; ++q) {
+            const uint32_t j = s0 + q;
+            if (j != i) vdiff = __fadd_rn(vdiff, foam_term(xi, vi, __ldg(pos + j), __ldg(vel_start + j)));
+          }
+        }
+  }
+  const uint32_t me = id[i];
+  float4 c;
+  if (color_dye(p, xi, vi, dens[i], add, vdiff, dye ? dye + me : nullptr, c)) clr[me] = c;
+}
+
 // ---- buffer API kernels ---------------------------------------------------
 
 __global__ void k_iota(uint32_t* __restrict__ a, uint32_t N) {
@@ -789,6 +831,8 @@ struct SphSystem {
   float* mlp_y = nullptr;            // N x 3 corrections
   float4* bk_vel = nullptr;          // velocity checkpoint for the fallback
   double* stats_host = nullptr;      // pinned, 4 per scene
+  float4* clr_out = nullptr;         // caller's colour buffer (original order) or null
+  float* dye_out = nullptr;          // caller's dye buffer (original order) or null
   std::vector<double> lr_ref[2];     // mean densities of the last two accepted steps
   int lr_refs = 0;                   // how many of lr_ref are valid for the current state
 };
@@ -891,6 +935,9 @@ int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr,
     launch_walks<true>(s, st, b, v, o, mark);
   else
     launch_walks<false>(s, st, b, v, o, mark);
+  if (s->clr_out)
+    k_color<<<gN, kBlock, 0, st>>>(sc, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->vel[v],
+                                   s->dens, s->start, s->count, s->id[b], s->clr_out, s->dye_out);
   mark();
   SPH_CUDA(cudaGetLastError(), "step kernels");
   s->cp = b;
@@ -1155,6 +1202,15 @@ int sph_set_graph_steps(SphSystem* s, uint32_t steps_per_graph) {
   SPH_CUDA(cudaStreamSynchronize(s->stream), "set_graph_steps: drain");
   drop_graphs(s);
   s->graph_steps = steps_per_graph;
+  return SPH_OK;
+}
+
+int sph_set_color_output(SphSystem* s, sph_float4* clr, float* dye) {
+  if (!s) return fail(SPH_ERR_ARG, "null handle");
+  if (!clr && dye) return fail(SPH_ERR_ARG, "set_color_output: dye needs a colour buffer");
+  s->clr_out = (float4*)clr;
+  s->dye_out = dye;
+  drop_graphs(s);  // the step graphs hold the old pointers
   return SPH_OK;
 }
 

@@ -222,6 +222,14 @@ class SPH:
     def set_graph_steps(self, steps: int) -> None:
         check(lib().sph_set_graph_steps(self._h, steps))
 
+    def set_color_output(self, clr=None, dye=None) -> None:
+        """Colour (float4) and dye (float) of every following step, written
+        into caller-owned device tensors of n records in original order;
+        None turns the output off.  The tensors must outlive their use."""
+        self._color_keep = (clr, dye)
+        p = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())  # noqa: E731
+        check(lib().sph_set_color_output(self._h, p(clr), p(dye)))
+
     WALK_THREADS = (64, 128, 256)
 
     def set_walk_shape(self, shape: int) -> None:
