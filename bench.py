@@ -350,6 +350,35 @@ def measure_learned(w, p, stream, fine_steps: int = 2000, substeps: int = 4, tol
                     "step with the drift correction and a zero network, no density check"}
 
 
+def measure_render(sysm, p, stream, width: int = 1920, height: int = 1080, iterations: int = 8,
+                   frames: int = 10):
+    """The headless renderer on the state the timed steps left: curvature
+    flow with `iterations` passes at width x height, wall time per frame
+    (each frame is synchronous; CUDA events bracket the frames)."""
+    import torch
+    from pibiti_gb300.render import Renderer, look_at, perspective
+    from pibiti_gb300.sph import ARRAY_POS
+    pos = torch.empty((sysm.n, 4), dtype=torch.float32, device="cuda")
+    sysm.get_array(ARRAY_POS, out=pos)
+    torch.cuda.synchronize()
+    mv = look_at((3.0, 2.6, 6.8), (3.0, 0.6, 0.85))
+    pr = perspective(60.0, width / height, 0.1, 20.0)
+    with Renderer(width, height) as r:
+        prm = r.params(mv, pr, radius=2.0 * p.particleR, method=1, iterations=iterations)
+        for _ in range(2):
+            r.frame_params(pos, prm)
+        t0 = time.perf_counter()
+        for _ in range(frames):
+            r.frame_params(pos, prm)
+        ms = 1e3 * (time.perf_counter() - t0) / frames
+        frags = r.fragments
+    return {"ms_per_frame": ms, "width": width, "height": height, "particles": sysm.n,
+            "method": "curvature flow", "iterations": iterations, "fragments": int(frags),
+            "fragments_per_s": frags / (ms / 1e3),
+            "note": "depth + thickness G-buffer in draw order, smoothing, shading; wall time "
+                    "of synchronous frames"}
+
+
 def workload_config(p, n=None):
     cfg = {"workload": "double dam break, 1,048,576 particles: two 64x128x64 lattices at "
                        "spacing 0.5h (h=0.0457 m) in a 6.0x3.4x1.7 m box, +-1% jitter, "
@@ -400,6 +429,7 @@ def main():
                     help="ensemble: the 256-scene batched ensemble (a separate measurement)")
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-form measurement")
+    ap.add_argument("--no-render", action="store_true", help="skip the render measurement")
     ap.add_argument("--save-state", metavar="NPZ",
                     help="profiling aid: run --warm-steps steps of the workload, save the state, exit")
     ap.add_argument("--stages", metavar="NPZ",
@@ -524,6 +554,7 @@ def main():
     e2e_value = job_throughput(n, args.e2e_steps, world, e2e_ms)
 
     learned = measure_learned(w, p, stream) if rank == 0 and not args.no_learned else None
+    render = measure_render(sysm, p, stream) if rank == 0 and not args.no_render else None
 
     st = sysm.stats()[0]
     flags = sysm.flags()
@@ -542,6 +573,7 @@ def main():
             "warm_ms_per_step": warm_ms,
             "wall_s_timed_loop": wall,
             "learned": learned,
+            "render": render,
             "state_check": {"kinetic_energy": st[0], "mean_density": st[1],
                             "max_density_dev": st[2], "nonfinite": st[3], "flags": flags},
         }

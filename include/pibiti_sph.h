@@ -352,6 +352,41 @@ int sph_drop_particles(const SimParams* params, const SphSceneInfo* info, int ra
    rotor angles advanced by one time step, the dye-clear countdown. */
 int sph_scene_advance(SimParams* params, const SphSceneMotion* motion);
 
+/* ======================================================================
+ * 5. Headless screen-space rendering (no reference ABI counterpart: the
+ *    reference renders through OpenGL, Graphics/render_particles.cpp)
+ * ==================================================================== */
+
+/* The reference's fluid pipeline in CUDA, into device buffers: point
+   sprites into a depth and thickness G-buffer in draw order (Gbuffer.vs,
+   Gbuffer.fs; depth test GL_LESS, blend SRC_ALPHA / ONE_MINUS_SRC_ALPHA),
+   `iterations` passes of curvature flow (CurvatureFlow.fs, method 1) or of
+   the bilateral filter (BilateralFilter.fs, method 2), then the shading of
+   ScreenSpaceRender.fs.  The cube map and the scene behind the fluid are
+   the constant colours env_color and background.  Depth is FP32 (the
+   reference's depth textures are the driver's choice). */
+#define SPH_RENDER_MAX_KERNEL_CENTER 16
+typedef struct SphRenderer SphRenderer;
+typedef struct {
+  float modelview[16], projection[16]; /* GL column-major */
+  float point_radius, point_scale;     /* m_ParRadius, m_ParScale (pixels at distance 1) */
+  int32_t method;                      /* RenderMethod: 0 none, 1 curvature flow, 2 bilateral */
+  int32_t iterations;                  /* nIter */
+  int32_t kernel_center;               /* KernelC (bilateral), <= SPH_RENDER_MAX_KERNEL_CENTER */
+  float sigma;                         /* DomainSigma (bilateral; the reference uses 0.01) */
+  float env_color[3], background[3];
+} SphRenderParams;
+int sph_render_create(int width, int height, SphRenderer** out);
+int sph_render_destroy(SphRenderer* renderer);
+/* One frame of n particles (device float4 positions).  Outputs (device,
+   width x height, row 0 at the bottom as GL's window coordinates; any may
+   be NULL): the smoothed depth (1.0 where nothing was drawn), the
+   thickness, the RGBA image.  *fragments (may be NULL) receives the number
+   of sprite fragments.  Synchronous. */
+int sph_render_frame(SphRenderer* renderer, const SphRenderParams* params, const sph_float4* pos,
+                     uint32_t n, float* depth_out, float* thickness_out, sph_float4* rgba_out,
+                     uint64_t* fragments);
+
 #ifdef __cplusplus
 }
 #endif

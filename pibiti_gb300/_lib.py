@@ -98,6 +98,9 @@ SIGNATURES = {
     "sph_scene_default": [P(SimParams), P(SceneInfo)],
     "sph_scene_default_index": [ctypes.c_char_p, P(i32)],
     "sph_scene_reset": [P(SimParams), P(SceneInfo), i32, ctypes.c_uint64, vp, vp, P(u32)],
+    "sph_render_create": [i32, i32, P(vp)],
+    "sph_render_destroy": [vp],
+    "sph_render_frame": [vp, vp, vp, u32, vp, vp, vp, P(ctypes.c_uint64)],
     "sph_scene_load_motion": [ctypes.c_char_p, i32, P(SceneMotion)],
     "sph_scene_parse_motion": [ctypes.c_char_p, P(SceneMotion)],
     "sph_emitter_particles": [P(Emitter), ctypes.c_float, vp, vp, u32, P(u32)],

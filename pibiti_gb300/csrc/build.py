@@ -21,7 +21,8 @@ ROOT = os.path.dirname(PKG)
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libpibiti_sph.so")
 
-CUDA_SOURCES = ["sph_stage.cu", "sph_scan.cu", "sph_system.cu", "sph_noalloc.cu", "sph_mlp.cu"]
+CUDA_SOURCES = ["sph_stage.cu", "sph_scan.cu", "sph_system.cu", "sph_noalloc.cu", "sph_mlp.cu",
+                "sph_render.cu"]
 HOST_SOURCES = ["scene.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
