@@ -177,6 +177,15 @@ int sph_set_graph_steps(SphSystem* sys, uint32_t steps_per_graph);
    form of both. */
 int sph_set_color_output(SphSystem* sys, sph_float4* clr, float* dye);
 
+/* Persistent stepping: with on != 0, sph_step(sys, k) runs its k steps as
+   one cooperative launch (all blocks resident, a grid barrier between the
+   stages, the same per-particle code as the launch-per-stage path, so the
+   same results bit for bit).  A barrier wait that does not end within its
+   poll limit sets bit 4 of sph_flags and the kernel returns early.  Needs
+   the neighbour masks (maxParInCell <= 21) and a device with cooperative
+   launch; not used while a colour output is set. */
+int sph_set_persistent(SphSystem* sys, int on);
+
 /* Launch shape of the density and force walks: 0 = 64 threads per block,
    1 = 128 (default), 2 = 256, each compiled for full occupancy at that size. */
 int sph_set_walk_shape(SphSystem* sys, uint32_t shape);

@@ -56,6 +56,15 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
+// A read of data that stays read-only for the whole kernel (kNC: through the
+// non-coherent path) or of data other blocks of the same (persistent)
+// kernel write between its stages (a plain load, ordered by the barrier).
+template <bool kNC, class T>
+__device__ __forceinline__ T ld(const T* p) {
+  if constexpr (kNC) return __ldg(p);
+  else return *p;
+}
+
 // Scene holding element i of a concatenation with offsets off[0..S].
 __device__ __forceinline__ int scene_of(const uint32_t* __restrict__ off, int S, uint32_t i) {
   int lo = 0, hi = S - 1;
@@ -66,12 +75,13 @@ __device__ __forceinline__ int scene_of(const uint32_t* __restrict__ off, int S,
   return lo;
 }
 
-__global__ void __launch_bounds__(kBlock)
-k_integrate_count(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S,
+// Integrate particle i, find its cell and take a rank in it with one
+// atomicAdd per group of lanes sharing the cell.  Called by all 32 lanes
+// of a warp for consecutive i (i >= N: the lane takes part but does nothing).
+__device__ __forceinline__ void integrate_count_item(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S,
                   uint32_t N, const float4* __restrict__ pos, const float4* __restrict__ vel,
                   uint32_t* __restrict__ key, uint32_t* __restrict__ rank,
-                  uint32_t* __restrict__ count, uint32_t* __restrict__ flags) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+                  uint32_t* __restrict__ count, uint32_t* __restrict__ flags, uint32_t i) {
   const bool valid = i < N;
   uint32_t gcell = 0xffffffffu;
   if (valid) {
@@ -94,6 +104,15 @@ k_integrate_count(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__
 }
 
 __global__ void __launch_bounds__(kBlock)
+k_integrate_count(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S,
+                  uint32_t N, const float4* __restrict__ pos, const float4* __restrict__ vel,
+                  uint32_t* __restrict__ key, uint32_t* __restrict__ rank,
+                  uint32_t* __restrict__ count, uint32_t* __restrict__ flags) {
+  integrate_count_item(sc, poff, S, N, pos, vel, key, rank, count, flags,
+                       blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(kBlock)
 k_scatter_ids(uint32_t N, const uint32_t* __restrict__ key, const uint32_t* __restrict__ rank,
               const uint32_t* __restrict__ id, const uint32_t* __restrict__ start,
               uint32_t* __restrict__ slot) {
@@ -108,16 +127,13 @@ k_scatter_ids(uint32_t N, const uint32_t* __restrict__ key, const uint32_t* __re
 // original index, the order the reference's stable sort gives within a cell.
 constexpr uint32_t kLinearRank = 32;
 
-__global__ void __launch_bounds__(kBlock)
-k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
+__device__ __forceinline__ void place_item(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
         const float4* __restrict__ pos, const float4* __restrict__ vel,
         const uint32_t* __restrict__ id, const uint32_t* __restrict__ key,
         const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
         const uint32_t* __restrict__ slot, float4* __restrict__ pos_out,
         float4* __restrict__ vel_out, uint32_t* __restrict__ id_out,
-        float4* __restrict__ vel_start = nullptr) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
+        float4* __restrict__ vel_start, uint32_t i) {
   const uint32_t c = key[i], s0 = start[c], n = count[c], me = id[i];
   uint32_t r = 0;
   if (n <= kLinearRank) {
@@ -139,6 +155,20 @@ k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   vel_out[dest] = make_float4(v.x, v.y, v.z, v4.w);
   id_out[dest] = me;
   if (vel_start) vel_start[dest] = v4;  // the velocity before gravity and the walls
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
+        const float4* __restrict__ pos, const float4* __restrict__ vel,
+        const uint32_t* __restrict__ id, const uint32_t* __restrict__ key,
+        const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
+        const uint32_t* __restrict__ slot, float4* __restrict__ pos_out,
+        float4* __restrict__ vel_out, uint32_t* __restrict__ id_out,
+        float4* __restrict__ vel_start = nullptr) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  place_item(sc, poff, S, N, pos, vel, id, key, start, count, slot, pos_out, vel_out, id_out,
+             vel_start, i);
 }
 
 // Launch shapes of the two walks: (threads per block, minimum resident
@@ -166,15 +196,12 @@ __device__ __forceinline__ float h2_out_of(const SimParams& p) {
   return __int_as_float(__float_as_int(__fmul_rn(p.h, p.h)) + 2);
 }
 
-template <bool kMask, int kThreads, int kMinBlocks>
-__global__ void __launch_bounds__(kThreads, kMinBlocks)
-k_density(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
+template <bool kMask, bool kNC = true>
+__device__ __forceinline__ void density_item(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
           const float4* __restrict__ pos, const uint32_t* __restrict__ start,
           const uint32_t* __restrict__ count, float* __restrict__ dens_out,
           float* __restrict__ pres_out, float2* __restrict__ dp_out,
-          unsigned long long* __restrict__ masks, uint32_t* __restrict__ flags) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
+          unsigned long long* __restrict__ masks, uint32_t* __restrict__ flags, uint32_t i) {
   const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
   const SimParams& p = d.p;
   const float4 xi = pos[i];
@@ -196,18 +223,18 @@ k_density(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, i
 #pragma unroll 1
       for (int x = x0; x <= x1; ++x) {
         const uint32_t c = row + (uint32_t)x;
-        uint32_t n = __ldg(count + c);
+        uint32_t n = ld<kNC>(count + c);
         if (n > maxpc) {
           trunc = true;
           n = maxpc;
         }
-        const uint32_t s0 = __ldg(start + c);
+        const uint32_t s0 = ld<kNC>(start + c);
         float cell = 0.f;
         uint32_t m = 0;
         // only the particle's own cell holds i
         const uint32_t self = (r == 4 && x == cx) ? i - s0 : 0xffffffffu;
         auto cand = [&](uint32_t k) {
-          const float4 xj = __ldg(pos + s0 + k);
+          const float4 xj = ld<kNC>(pos + s0 + k);
           const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
           const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
           if (r2 < h2) {
@@ -240,6 +267,18 @@ k_density(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, i
   dp_out[i] = make_float2(__frcp_rn(dens), pres);  // the force pass's per-neighbour record
 }
 
+template <bool kMask, int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+k_density(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
+          const float4* __restrict__ pos, const uint32_t* __restrict__ start,
+          const uint32_t* __restrict__ count, float* __restrict__ dens_out,
+          float* __restrict__ pres_out, float2* __restrict__ dp_out,
+          unsigned long long* __restrict__ masks, uint32_t* __restrict__ flags) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  density_item<kMask>(sc, poff, S, N, pos, start, count, dens_out, pres_out, dp_out, masks, flags, i);
+}
+
 // Learned-corrector features of particle i (SPH_MLP_IN = 16), from the
 // neighbours the force pass visits with r < h, weight w = ((h - r)/h)^2:
 //   0 rho/rho0 - 1            1 p / (rho0 g h)          2 neighbours / 64
@@ -260,15 +299,12 @@ struct FeatOut {
   const float* stats;       // mean[16], inv_std[16]
 };
 
-template <bool kMask, int kThreads, int kMinBlocks, bool kFeat>
-__global__ void __launch_bounds__(kThreads, kFeat ? kMinBlocks * 3 / 4 : kMinBlocks)
-k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
+template <bool kMask, bool kFeat, bool kNC = true>
+__device__ __forceinline__ void force_item(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
         const float4* __restrict__ pos, const float4* __restrict__ vel,
         const float* __restrict__ dens, const float2* __restrict__ dp,
         const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
-        const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out, FeatOut fo) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
+        const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out, FeatOut fo, uint32_t i) {
   const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
   const SimParams& p = d.p;
   const float4 xi = pos[i], vi = vel[i];
@@ -304,23 +340,23 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   // Pair term of candidate j (the masks already hold dist2 < h2_out):
   // returns whether r < h, with the term in f.
   auto term = [&](uint32_t j, float3& f, bool with_feat) -> bool {
-    const float4 xj = __ldg(pos + j);
+    const float4 xj = ld<kNC>(pos + j);
     const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
     const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
-    const float4 vj = __ldg(vel + j);
-    const float2 dpj = __ldg(dp + j);
+    const float4 vj = ld<kNC>(vel + j);
+    const float2 dpj = ld<kNC>(dp + j);
     const bool in = force_term(k, vi, inv_di, pi, vj, dpj.x, dpj.y, rx, ry, rz, dist2, f);
     if (kFeat && with_feat) feat(vj, rx, ry, rz, dist2);
     return in;
   };
   // Candidate j of the unmasked walk: skipped beyond h2_out before the loads.
   auto pair = [&](uint32_t j, float3& cell) {
-    const float4 xj = __ldg(pos + j);
+    const float4 xj = ld<kNC>(pos + j);
     const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
     const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
     if (!(dist2 >= k.h2_out)) {
-      const float4 vj = __ldg(vel + j);
-      const float2 dpj = __ldg(dp + j);
+      const float4 vj = ld<kNC>(vel + j);
+      const float2 dpj = ld<kNC>(dp + j);
       force_pair_near(k, vi, inv_di, pi, vj, dpj.x, dpj.y, rx, ry, rz, dist2, cell);
       if (kFeat) feat(vj, rx, ry, rz, dist2);
     }
@@ -344,11 +380,11 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
       if (!m) continue;
       const uint32_t row = d.c_off + (uint32_t)(z * (int)p.gridSize_yx + y * gx) + (uint32_t)x0;
       const int nc = x1 - x0 + 1;
-      const uint32_t n0 = min(__ldg(count + row), maxpc);
-      const uint32_t n1 = nc > 1 ? min(__ldg(count + row + 1), maxpc) : 0u;
-      const uint32_t s0 = __ldg(start + row);
-      const uint32_t s1 = nc > 1 ? __ldg(start + row + 1) : 0u;
-      const uint32_t s2 = nc > 2 ? __ldg(start + row + 2) : 0u;
+      const uint32_t n0 = min(ld<kNC>(count + row), maxpc);
+      const uint32_t n1 = nc > 1 ? min(ld<kNC>(count + row + 1), maxpc) : 0u;
+      const uint32_t s0 = ld<kNC>(start + row);
+      const uint32_t s1 = nc > 1 ? ld<kNC>(start + row + 1) : 0u;
+      const uint32_t s2 = nc > 2 ? ld<kNC>(start + row + 2) : 0u;
       const uint32_t b1 = n0, b2 = n0 + n1;
       int cur = -1;
       auto cell_of_bit = [&](uint32_t b) { return b >= b2 ? 2 : (b >= b1 ? 1 : 0); };
@@ -399,8 +435,8 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
 #pragma unroll 1
       for (int x = x0; x <= x1; ++x) {
         const uint32_t c = row + (uint32_t)x;
-        const uint32_t n = min(__ldg(count + c), maxpc);
-        const uint32_t s0 = __ldg(start + c);
+        const uint32_t n = min(ld<kNC>(count + c), maxpc);
+        const uint32_t s0 = ld<kNC>(start + c);
 #pragma unroll 4
         for (uint32_t q = 0; q < n; ++q)
           if (s0 + q != i) pair(s0 + q, cell);
@@ -456,6 +492,18 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
       o[1] = make_uint4(u[4], u[5], u[6], u[7]);
     }
   }
+}
+
+template <bool kMask, int kThreads, int kMinBlocks, bool kFeat>
+__global__ void __launch_bounds__(kThreads, kFeat ? kMinBlocks * 3 / 4 : kMinBlocks)
+k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
+        const float4* __restrict__ pos, const float4* __restrict__ vel,
+        const float* __restrict__ dens, const float2* __restrict__ dp,
+        const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
+        const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out, FeatOut fo) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  force_item<kMask, kFeat>(sc, poff, S, N, pos, vel, dens, dp, start, count, masks, vel_out, fo, i);
 }
 
 // After a coarse step of dt_c = n dt (sorted order).  Within a step,
@@ -683,6 +731,224 @@ __global__ void __launch_bounds__(kBlock) k_stats(const SceneDesc* __restrict__ 
   add(s, ke, rho, dev, bad);
 }
 
+// ---- persistent step ------------------------------------------------------
+// K whole steps in one cooperative launch: every block runs every stage as a
+// grid-stride loop over the same per-item device functions the separate
+// kernels use, with a grid barrier between stages, so the results are those
+// of enqueue_step bit for bit.  The launch is cooperative, so all blocks are
+// resident; the barrier's waits are bounded: after kBarrierSpins polls a
+// block sets bit 4 of `flags` and the barrier status, and every block leaves
+// at its next barrier.
+constexpr int kPThreads = 256;
+constexpr int kPWarps = kPThreads / 32;
+constexpr uint32_t kPTile = kPThreads * 8;            // scan tile
+constexpr uint32_t kPBlockSortMax = kPWarps * kWarpSortMax;  // keys a block sorts in shared memory
+constexpr uint32_t kBarrierSpins = 1u << 24;
+constexpr uint32_t kFlagBarrier = 4u;
+
+struct PersistArgs {
+  const SceneDesc* sc;
+  const uint32_t* poff;
+  int S;
+  uint32_t N, C;
+  float4 *pos0, *pos1, *vel0, *vel1;
+  uint32_t *id0, *id1;
+  uint32_t *key, *rank, *slot, *count, *start, *tsum;
+  float *dens, *pres;
+  float2* dp;
+  unsigned long long* masks;
+  uint32_t* flags;
+  uint32_t *sort_list, *sort_counters, *big_list, *sort_scratch;
+  uint32_t* bar;  // [arrived, generation, status]
+  uint32_t steps;
+  int cp, cv;
+};
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Sense-reversing grid barrier: the last block to arrive resets the count
+// and advances the generation; the others poll the generation (acquire).
+__device__ bool grid_barrier(uint32_t* bar, uint32_t* flags) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t g = ld_acquire(bar + 1);
+    __threadfence();
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      uint32_t spins = 0;
+      while (ld_acquire(bar + 1) == g) {
+        if (++spins > kBarrierSpins) {
+          atomicOr(bar + 2, 1u);
+          atomicOr(flags, kFlagBarrier);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *((volatile uint32_t*)(bar + 2)) == 0;
+}
+
+// Exclusive scan over the block of one value per thread; *total gets the sum.
+__device__ __forceinline__ uint32_t p_block_scan(uint32_t v, uint32_t* wtot, uint32_t* total) {
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if ((int)lane >= o) x += y;
+  }
+  if (lane == 31) wtot[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t t = lane < kPWarps ? wtot[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if ((int)lane >= o) t += y;
+    }
+    if (lane < kPWarps) wtot[lane] = t;  // inclusive warp offsets
+  }
+  __syncthreads();
+  const uint32_t off = w ? wtot[w - 1] : 0u;
+  *total = wtot[kPWarps - 1];
+  __syncthreads();
+  return off + x - v;
+}
+
+__global__ void __launch_bounds__(kPThreads, 4) k_persistent(PersistArgs a) {
+  extern __shared__ uint32_t psm[];  // kPWarps x kWarpSortMax words
+  __shared__ uint32_t wtot[32];
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
+  const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const uint32_t gwarp = tid >> 5, nwarps = nthr >> 5;
+  const uint32_t tiles = (a.C + kPTile - 1) / kPTile;
+  float4* vel_v = a.cv ? a.vel1 : a.vel0;
+  float4* vel_o = a.cv ? a.vel0 : a.vel1;
+  int cp = a.cp;
+  for (uint32_t step = 0; step < a.steps; ++step) {
+    float4 *pa = cp ? a.pos1 : a.pos0, *pb = cp ? a.pos0 : a.pos1;
+    uint32_t *ia = cp ? a.id1 : a.id0, *ib = cp ? a.id0 : a.id1;
+    // clear the cell counts and the sort lists
+    for (uint32_t c = tid; c < a.C; c += nthr) a.count[c] = 0u;
+    if (tid == 0) a.sort_counters[0] = a.sort_counters[1] = 0u;
+    if (!grid_barrier(a.bar, a.flags)) return;
+    // integrate and count (whole warps over consecutive particles)
+    for (uint32_t base = gwarp * 32; base < a.N; base += nwarps * 32)
+      integrate_count_item(a.sc, a.poff, a.S, a.N, pa, vel_v, a.key, a.rank, a.count, a.flags, base + lane);
+    if (!grid_barrier(a.bar, a.flags)) return;
+    // exclusive scan count -> start: tile sums, their scan (block 0), tiles
+    for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+      uint32_t sum = 0, tot;
+      for (uint32_t k = 0; k < 8; ++k) {
+        const uint32_t c = t * kPTile + threadIdx.x * 8 + k;
+        if (c < a.C) sum += a.count[c];
+      }
+      p_block_scan(sum, wtot, &tot);
+      if (threadIdx.x == 0) a.tsum[t] = tot;
+    }
+    if (!grid_barrier(a.bar, a.flags)) return;
+    if (blockIdx.x == 0) {
+      uint32_t carry = 0;
+      for (uint32_t t0 = 0; t0 < tiles; t0 += kPThreads) {
+        const uint32_t t = t0 + threadIdx.x;
+        const uint32_t v = t < tiles ? a.tsum[t] : 0u;
+        uint32_t tot;
+        const uint32_t e = p_block_scan(v, wtot, &tot);
+        if (t < tiles) a.tsum[t] = carry + e;
+        carry += tot;
+      }
+    }
+    if (!grid_barrier(a.bar, a.flags)) return;
+    for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+      uint32_t v[8], sum = 0, tot;
+      for (uint32_t k = 0; k < 8; ++k) {
+        const uint32_t c = t * kPTile + threadIdx.x * 8 + k;
+        v[k] = c < a.C ? a.count[c] : 0u;
+        sum += v[k];
+      }
+      uint32_t run = p_block_scan(sum, wtot, &tot) + a.tsum[t];
+      for (uint32_t k = 0; k < 8; ++k) {
+        const uint32_t c = t * kPTile + threadIdx.x * 8 + k;
+        if (c < a.C) a.start[c] = run;
+        run += v[k];
+      }
+    }
+    if (!grid_barrier(a.bar, a.flags)) return;
+    // ids into their cells; cells that need their ids sorted
+    for (uint32_t i = tid; i < a.N; i += nthr) a.slot[a.start[a.key[i]] + a.rank[i]] = ia[i];
+    for (uint32_t base = gwarp * 32; base < a.C; base += nwarps * 32) {
+      const uint32_t c = base + lane;
+      const uint32_t n = c < a.C ? a.count[c] : 0u;
+      const bool mid = n > kLinearRank && n <= kWarpSortMax, big = n > kWarpSortMax;
+      const uint32_t bm = __ballot_sync(0xffffffffu, mid), bb = __ballot_sync(0xffffffffu, big);
+      uint32_t base_m = 0, base_b = 0;
+      if (lane == 0) {
+        if (bm) base_m = atomicAdd(a.sort_counters + 0, (uint32_t)__popc(bm));
+        if (bb) base_b = atomicAdd(a.sort_counters + 1, (uint32_t)__popc(bb));
+      }
+      base_m = __shfl_sync(0xffffffffu, base_m, 0);
+      base_b = __shfl_sync(0xffffffffu, base_b, 0);
+      const uint32_t below = (1u << lane) - 1u;
+      if (mid) a.sort_list[base_m + (uint32_t)__popc(bm & below)] = c;
+      if (big) a.big_list[base_b + (uint32_t)__popc(bb & below)] = c;
+    }
+    if (!grid_barrier(a.bar, a.flags)) return;
+    // sort: a warp per listed cell, then a block per big cell
+    {
+      const uint32_t nl = *((volatile uint32_t*)a.sort_counters);
+      uint32_t* b = psm + wib * kWarpSortMax;
+      for (uint32_t q = gwarp; q < nl; q += nwarps) {
+        const uint32_t c = a.sort_list[q], n = a.count[c], s0 = a.start[c], m = pow2_at_least(n);
+        for (uint32_t k = lane; k < m; k += 32) b[k] = k < n ? a.slot[s0 + k] : 0xffffffffu;
+        __syncwarp();
+        bitonic(b, m, lane, 32, [] { __syncwarp(); });
+        for (uint32_t k = lane; k < n; k += 32) a.slot[s0 + k] = b[k];
+        __syncwarp();
+      }
+      __syncthreads();
+      const uint32_t nb = *((volatile uint32_t*)(a.sort_counters + 1));
+      for (uint32_t q = blockIdx.x; q < nb; q += gridDim.x) {
+        const uint32_t c = a.big_list[q], n = a.count[c], s0 = a.start[c], m = pow2_at_least(n);
+        uint32_t* bb = m <= kPBlockSortMax ? psm : a.sort_scratch + 2 * (size_t)s0;
+        for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) bb[k] = k < n ? a.slot[s0 + k] : 0xffffffffu;
+        __syncthreads();
+        if (m <= kPBlockSortMax)
+          bitonic(bb, m, threadIdx.x, blockDim.x, [] { __syncthreads(); });
+        else
+          bitonic(bb, m, threadIdx.x, blockDim.x, [] {
+            __threadfence_block();
+            __syncthreads();
+          });
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) a.slot[s0 + k] = bb[k];
+        __syncthreads();
+      }
+    }
+    if (!grid_barrier(a.bar, a.flags)) return;
+    for (uint32_t i = tid; i < a.N; i += nthr)
+      place_item(a.sc, a.poff, a.S, a.N, pa, vel_v, ia, a.key, a.start, a.count, a.slot, pb, vel_o, ib,
+                 nullptr, i);
+    if (!grid_barrier(a.bar, a.flags)) return;
+    for (uint32_t i = tid; i < a.N; i += nthr)
+      density_item<true, false>(a.sc, a.poff, a.S, a.N, pb, a.start, a.count, a.dens, a.pres, a.dp, a.masks,
+                         a.flags, i);
+    if (!grid_barrier(a.bar, a.flags)) return;
+    const FeatOut no_feat = {nullptr, nullptr, nullptr};
+    for (uint32_t i = tid; i < a.N; i += nthr)
+      force_item<true, false, false>(a.sc, a.poff, a.S, a.N, pb, vel_o, a.dens, a.dp, a.start, a.count,
+                              a.masks, vel_v, no_feat, i);
+    if (!grid_barrier(a.bar, a.flags)) return;
+    cp = 1 - cp;
+  }
+}
+
 }  // namespace
 }  // namespace sph
 
@@ -734,6 +1000,10 @@ struct SphSystem {
   float* mlp_y = nullptr;            // N x 3 corrections
   float4* bk_vel = nullptr;          // velocity checkpoint for the fallback
   double* stats_host = nullptr;      // pinned, 4 per scene
+  bool persistent = false;           // steps as one cooperative launch (k_persistent)
+  unsigned persist_grid = 0;
+  uint32_t* ptsum = nullptr;         // scan tile sums of the persistent step
+  uint32_t* pbar = nullptr;          // its grid barrier: arrived, generation, status
   float4* clr_out = nullptr;         // caller's colour buffer (original order) or null
   float* dye_out = nullptr;          // caller's dye buffer (original order) or null
   std::vector<double> lr_ref[2];     // mean densities of the last two accepted steps
@@ -873,7 +1143,7 @@ void free_all(SphSystem* s) {
   void* bufs[] = {s->d_scenes, s->d_poff, s->d_coff, s->pos[0], s->pos[1], s->vel[0], s->vel[1],
                   s->id[0], s->id[1], s->key, s->rank, s->slot, s->count, s->start, s->scan_tmp,
                   s->dens, s->pres, s->dp, s->masks, s->flags, s->stats, s->staging, s->d_coarse,
-                  s->mlp_img, s->mlp_aux, s->feat, s->mlp_y, s->bk_vel, s->vstart, s->hist,
+                  s->mlp_img, s->mlp_aux, s->feat, s->mlp_y, s->bk_vel, s->vstart, s->hist, s->ptsum, s->pbar,
                   s->big_list, s->sort_counters, s->sort_list, s->sort_scratch};
   for (void* p : bufs)
     if (p) cudaFree(p);
@@ -1084,9 +1354,80 @@ int sph_get_array(SphSystem* s, uint32_t which, sph_float4* out, int dst_on_devi
   return SPH_OK;
 }
 
+static int persistent_steps(SphSystem* s, uint32_t steps) {
+  PersistArgs a;
+  a.sc = s->d_scenes;
+  a.poff = s->d_poff;
+  a.S = s->S;
+  a.N = s->N;
+  a.C = s->C;
+  a.pos0 = s->pos[0];
+  a.pos1 = s->pos[1];
+  a.vel0 = s->vel[0];
+  a.vel1 = s->vel[1];
+  a.id0 = s->id[0];
+  a.id1 = s->id[1];
+  a.key = s->key;
+  a.rank = s->rank;
+  a.slot = s->slot;
+  a.count = s->count;
+  a.start = s->start;
+  a.tsum = s->ptsum;
+  a.dens = s->dens;
+  a.pres = s->pres;
+  a.dp = s->dp;
+  a.masks = s->masks;
+  a.flags = s->flags;
+  a.sort_list = s->sort_list;
+  a.sort_counters = s->sort_counters;
+  a.big_list = s->big_list;
+  a.sort_scratch = s->sort_scratch;
+  a.bar = s->pbar;
+  a.steps = steps;
+  a.cp = s->cp;
+  a.cv = s->cv;
+  SPH_CUDA(cudaMemsetAsync(s->pbar, 0, 3 * sizeof(uint32_t), s->stream), "persistent: barrier");
+  void* args[] = {&a};
+  SPH_CUDA(cudaLaunchCooperativeKernel((const void*)k_persistent, dim3(s->persist_grid), dim3(kPThreads),
+                                       args, kPWarps * kWarpSortMax * sizeof(uint32_t), s->stream),
+           "persistent step launch");
+  if (steps & 1) s->cp = 1 - s->cp;
+  return SPH_OK;
+}
+
+int sph_set_persistent(SphSystem* s, int on) {
+  if (!s) return fail(SPH_ERR_ARG, "null handle");
+  if (!on) {
+    s->persistent = false;
+    return SPH_OK;
+  }
+  if (!s->masks) return fail(SPH_ERR_UNSUPPORTED, "set_persistent: needs the neighbour masks (maxParInCell <= 21)");
+  int dev = 0, sms = 0, per_sm = 0, coop = 0;
+  SPH_CUDA(cudaGetDevice(&dev), "set_persistent");
+  SPH_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev), "set_persistent");
+  if (!coop) return fail(SPH_ERR_UNSUPPORTED, "set_persistent: no cooperative launch on this device");
+  SPH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "set_persistent");
+  SPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_persistent, kPThreads,
+                                                         kPWarps * kWarpSortMax * sizeof(uint32_t)),
+           "set_persistent: occupancy");
+  if (per_sm < 1) return fail(SPH_ERR_UNSUPPORTED, "set_persistent: kernel does not fit an SM");
+  if (!s->ptsum) SPH_TRY(dalloc(&s->ptsum, (s->C + kPTile - 1) / kPTile + 1, "persistent tile sums"));
+  if (!s->pbar) SPH_TRY(dalloc(&s->pbar, 3, "persistent barrier"));
+  s->persist_grid = (unsigned)(per_sm * sms);
+  s->persistent = true;
+  return SPH_OK;
+}
+
 int sph_step(SphSystem* s, uint32_t steps) {
   if (!s) return fail(SPH_ERR_ARG, "null handle");
   s->lr_refs = 0;  // the learned step's density history no longer applies
+  if (s->persistent && !s->clr_out) {
+    if (steps) {
+      SPH_TRY(persistent_steps(s, steps));
+      s->stepped = true;
+    }
+    return SPH_OK;
+  }
   uint32_t done = 0;
   const uint32_t gs = s->graph_steps;
   if (steps >= gs) {

@@ -230,6 +230,10 @@ class SPH:
         p = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())  # noqa: E731
         check(lib().sph_set_color_output(self._h, p(clr), p(dye)))
 
+    def set_persistent(self, on: bool = True) -> None:
+        """update(k) as one cooperative launch of k steps (same results)."""
+        check(lib().sph_set_persistent(self._h, int(on)))
+
     WALK_THREADS = (64, 128, 256)
 
     def set_walk_shape(self, shape: int) -> None:
