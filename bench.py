@@ -241,6 +241,22 @@ def run_ensemble(args):
     value = sysm.n * steps / (ms / 1e3)
     st = sysm.stats()
     sysm.close()
+    # the same steps as one persistent cooperative launch, from the same start
+    with SPH(ps, stream=stream) as ph:
+        ph.set_array(ARRAY_POS, e.pos)
+        ph.set_array(ARRAY_VEL, e.vel)
+        ph.set_persistent(True)
+        ph.update(args.warmup)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        ph.update(steps)  # one launch
+        p1.record(stream)
+        torch.cuda.synchronize()
+        pms = p0.elapsed_time(p1)
+        persistent = {"value": ph.n * steps / (pms / 1e3), "unit": UNIT, "ms_per_step": pms / steps,
+                      "barrier_timeout": bool(ph.flags() & 4),
+                      "note": f"{steps} steps in one cooperative launch (grid barrier between stages)"}
     # the same scenes, one handle each, for the first 32 scenes
     sub = 32
     t_sep, n_sep = 0.0, 0
@@ -271,6 +287,7 @@ def run_ensemble(args):
                    "graph": f"{steps} steps captured as one CUDA graph, one launch"},
         "autotune": {"chosen_threads": SPH.WALK_THREADS[chosen], "ms_per_step": tune_ms},
         "separate_handles": {"scenes": sub, "value": n_sep / t_sep, "unit": UNIT},
+        "persistent": persistent,
         "clocks": clk,
         "state_check": {"max_density_dev": float(st[:, 2].max()), "nonfinite": float(st[:, 3].sum())},
     }
