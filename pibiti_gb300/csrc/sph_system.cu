@@ -663,21 +663,32 @@ __global__ void __launch_bounds__(kBlock) k_stats(const SceneDesc* __restrict__ 
                                                   const float4* __restrict__ vel,
                                                   const float* __restrict__ dens,
                                                   double* __restrict__ acc) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   int s = -1;
   float ke = 0.f, rho = 0.f, dev = 0.f, bad = 0.f;
-  if (i < N) {
-    s = S == 1 ? 0 : scene_of(poff, S, i);
-    const SimParams& p = sc[s].p;
+  auto one = [&](uint32_t i, int sc_) {
+    const SimParams& p = sc[sc_].p;
     const float4 x = pos[i], v = vel[i];
-    ke = 0.5f * p.particleMass * (v.x * v.x + v.y * v.y + v.z * v.z);
-    rho = dens ? dens[i] : 0.f;
-    dev = dens ? fabsf(rho / p.restDensity - 1.f) : 0.f;
-    bad = (float)(!isfinite(x.x) + !isfinite(x.y) + !isfinite(x.z) + !isfinite(v.x) +
-                  !isfinite(v.y) + !isfinite(v.z));
-    if (!(ke == ke) || isinf(ke)) ke = 0.f;
-    if (!(rho == rho) || isinf(rho)) rho = 0.f;
-    if (!(dev == dev) || isinf(dev)) dev = 0.f;
+    float k = 0.5f * p.particleMass * (v.x * v.x + v.y * v.y + v.z * v.z);
+    float r = dens ? dens[i] : 0.f;
+    float dv = dens ? fabsf(r / p.restDensity - 1.f) : 0.f;
+    bad += (float)(!isfinite(x.x) + !isfinite(x.y) + !isfinite(x.z) + !isfinite(v.x) +
+                   !isfinite(v.y) + !isfinite(v.z));
+    if (!(k == k) || isinf(k)) k = 0.f;
+    if (!(r == r) || isinf(r)) r = 0.f;
+    if (!(dv == dv) || isinf(dv)) dv = 0.f;
+    ke += k;
+    rho += r;
+    dev = fmaxf(dev, dv);
+  };
+  if (S == 1) {  // grid-stride: each thread sums a few particles
+    s = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) one(i, 0);
+  } else {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) {
+      s = scene_of(poff, S, i);
+      one(i, s);
+    }
   }
   auto warp_sum = [](float& a, float& b, float& c, float& d) {
     for (int o = 16; o > 0; o >>= 1) {
@@ -969,6 +980,7 @@ struct SphSystem {
   uint32_t *big_list = nullptr, *sort_scratch = nullptr;
   uint32_t *sort_list = nullptr, *sort_counters = nullptr;  // counters: list, big_list sizes
   unsigned big_blocks = 1, sort_blocks = 1;
+  int sms = 1;                       // multiprocessors of the device
   uint32_t *count = nullptr, *start = nullptr, *scan_tmp = nullptr;
   float *dens = nullptr, *pres = nullptr;
   float2* dp = nullptr;               // per particle: 1/density, pressure (force pass)
@@ -1000,6 +1012,8 @@ struct SphSystem {
   float* mlp_y = nullptr;            // N x 3 corrections
   float4* bk_vel = nullptr;          // velocity checkpoint for the fallback
   double* stats_host = nullptr;      // pinned, 4 per scene
+  cudaGraphExec_t lgraph[2] = {nullptr, nullptr};  // one learned coarse step, by cp parity
+  uint64_t lgraph_key = 0;           // substeps and drift factor the learned graphs hold
   bool persistent = false;           // steps as one cooperative launch (k_persistent)
   unsigned persist_grid = 0;
   uint32_t* ptsum = nullptr;         // scan tile sums of the persistent step
@@ -1033,6 +1047,28 @@ void drop_graphs(SphSystem* s) {
       cudaGraphExecDestroy(g);
       g = nullptr;
     }
+  for (auto& g : s->lgraph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+inline uint32_t float_bits(float f) {
+  uint32_t u;
+  memcpy(&u, &f, sizeof(u));
+  return u;
+}
+
+// The stats kernel over the current state (into s->stats, cleared by the
+// caller).  A single scene is reduced grid-stride by a few blocks per SM, so
+// the FP64 atomics on the four totals stay few.
+int launch_stats(SphSystem* s, cudaStream_t st) {
+  const unsigned blocks = s->S == 1 ? std::min(grid_for(s->N, kBlock), 4u * (unsigned)s->sms)
+                                    : grid_for(s->N, kBlock);
+  k_stats<<<blocks, kBlock, 0, st>>>(s->d_scenes, s->d_poff, s->S, s->N, s->pos[s->cp], s->vel[s->cv],
+                                     s->stepped ? s->dens : nullptr, s->stats);
+  return cuda_check(cudaGetLastError(), "stats kernel");
 }
 
 // What one enqueued step uses besides the handle's buffers.
@@ -1222,6 +1258,7 @@ int create(const SimParams* scenes, uint32_t count, SphSystem** out) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     s->big_blocks = (unsigned)(sms > 0 ? sms : 1);
+    s->sms = sms > 0 ? sms : 1;
     s->sort_blocks = (unsigned)(sms > 0 ? 8 * sms : 8);
   }
   if (rc == SPH_OK) {
@@ -1302,6 +1339,7 @@ int sph_set_params(SphSystem* s, uint32_t scene, const SimParams* p) {
     return fail(SPH_ERR_PARAMS, "set_params: particle count and grid cannot change");
   SPH_TRY(validate_params(*p, true));
   s->params[scene] = *p;
+  s->coarse_sub = 0;  // the learned step's coarse table is rebuilt from the new parameters
   return upload_scenes(s);
 }
 
@@ -1631,22 +1669,74 @@ int sph_learned_step(SphSystem* s, uint32_t coarse_steps, uint32_t substeps, flo
   o.vel_start = s->vstart;
   o.feat = true;
   o.fo = {nullptr, s->feat, s->mlp_aux};
-  for (uint32_t k = 0; k < coarse_steps; ++k) {
+  if (!s->stats_host)
+    SPH_CUDA(cudaMallocHost((void**)&s->stats_host, sizeof(double) * 4 * s->S), "stats host buffer");
+  // One coarse step on `st`: checkpoint, featured step, MLP, correction, and
+  // the per-scene stats copied to the pinned host buffer.  Advances s->cp.
+  auto enqueue_coarse = [&](cudaStream_t st) -> int {
     // A step reads pos[cp] and id[cp] and writes the other pair, so only
     // the velocity (overwritten by the force pass) needs a checkpoint.
-    const int cp0 = s->cp, cv0 = s->cv;
-    SPH_CUDA(cudaMemcpyAsync(s->bk_vel, s->vel[cv0], sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, s->stream), "checkpoint");
-    SPH_TRY(enqueue_step(s, s->stream, nullptr, &o));
-    SPH_TRY(sph_mlp_forward(s->mlp_img, s->feat, s->N, s->mlp_y, s->stream));
-    k_apply_correction<<<grid_for(s->N, kBlock), kBlock, 0, s->stream>>>(
+    SPH_CUDA(cudaMemcpyAsync(s->bk_vel, s->vel[s->cv], sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, st), "checkpoint");
+    SPH_TRY(enqueue_step(s, st, nullptr, &o));
+    SPH_TRY(sph_mlp_forward(s->mlp_img, s->feat, s->N, s->mlp_y, st));
+    k_apply_correction<<<grid_for(s->N, kBlock), kBlock, 0, st>>>(
         s->d_coarse, s->d_poff, s->S, s->N, s->mlp_y, s->mlp_aux + 32, drift, jerk, s->vstart,
         s->vel[1 - s->cv], s->id[s->cp], s->hist, s->hist_valid, s->pos[s->cp], s->vel[s->cv]);
     SPH_CUDA(cudaGetLastError(), "apply correction");
+    SPH_CUDA(cudaMemsetAsync(s->stats, 0, sizeof(double) * 4 * s->S, st), "stats clear");
+    SPH_TRY(launch_stats(s, st));
+    SPH_CUDA(cudaMemcpyAsync(s->stats_host, s->stats, sizeof(double) * 4 * s->S, cudaMemcpyDeviceToHost, st),
+             "stats copy");
+    return SPH_OK;
+  };
+  // Without the jerk term (whose history flag changes from step to step)
+  // the coarse step is replayed as a CUDA graph, one per buffer parity.
+  const bool use_graph = jerk == 0.f;
+  const uint64_t key = ((uint64_t)substeps << 32) | (uint64_t)float_bits(drift);
+  if (use_graph && s->lgraph_key != key) {
+    for (auto& g : s->lgraph)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+    s->lgraph_key = key;
+  }
+  for (uint32_t k = 0; k < coarse_steps; ++k) {
+    const int cp0 = s->cp, cv0 = s->cv;
+    if (use_graph) {
+      if (!s->lgraph[cp0]) {
+        if (!s->cap_stream)
+          SPH_CUDA(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking), "capture stream");
+        SPH_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        const int rc = enqueue_coarse(s->cap_stream);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
+        s->cp = cp0;
+        if (rc != SPH_OK) {
+          if (g) cudaGraphDestroy(g);
+          return rc;
+        }
+        SPH_CUDA(e, "end capture");
+        const cudaError_t ie = cudaGraphInstantiate(&s->lgraph[cp0], g, 0);
+        cudaGraphDestroy(g);
+        SPH_CUDA(ie, "instantiate learned step graph");
+      }
+      SPH_CUDA(cudaGraphLaunch(s->lgraph[cp0], s->stream), "learned step graph launch");
+      s->cp = 1 - cp0;
+      s->stepped = true;
+    } else {
+      SPH_TRY(enqueue_coarse(s->stream));
+    }
     s->hist_valid = jerk != 0.f;
+    SPH_CUDA(cudaStreamSynchronize(s->stream), "learned step sync");
+    st.assign(s->stats_host, s->stats_host + 4 * s->S);
+    for (int i = 0; i < s->S; ++i) {
+      const double n = s->poff[i + 1] - s->poff[i];
+      st[4 * i + 1] = n ? st[4 * i + 1] / n : 0.0;
+    }
     // density-deviation check, per scene: the mean density of the step may
     // depart from the linear extrapolation of the last two accepted steps
     // by at most tol (relative), and nothing may be NaN/Inf
-    SPH_TRY(scene_stats(s, st));
     bool ok = true;
     for (int i = 0; i < s->S && ok; ++i) {
       if (st[4 * i + 3] != 0.0 || !(st[4 * i + 1] == st[4 * i + 1])) ok = false;
@@ -1744,10 +1834,7 @@ int sph_get_fields(SphSystem* s, float* density, float* pressure, int dst_on_dev
 int sph_stats(SphSystem* s, double* out) {
   if (!s || !out) return fail(SPH_ERR_ARG, "stats: bad arguments");
   SPH_CUDA(cudaMemsetAsync(s->stats, 0, sizeof(double) * 4 * s->S, s->stream), "stats clear");
-  k_stats<<<grid_for(s->N, kBlock), kBlock, 0, s->stream>>>(s->d_scenes, s->d_poff, s->S, s->N,
-                                                            s->pos[s->cp], s->vel[s->cv],
-                                                            s->stepped ? s->dens : nullptr, s->stats);
-  SPH_CUDA(cudaGetLastError(), "stats kernel");
+  SPH_TRY(launch_stats(s, s->stream));
   if (!s->stats_host)
     SPH_CUDA(cudaMallocHost((void**)&s->stats_host, sizeof(double) * 4 * s->S), "stats host buffer");
   SPH_CUDA(cudaMemcpyAsync(s->stats_host, s->stats, sizeof(double) * 4 * s->S,

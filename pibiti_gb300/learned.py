@@ -361,7 +361,10 @@ def main(argv=None) -> int:
     import torch
     from . import configs
     ap = argparse.ArgumentParser()
-    ap.add_argument("cmd", choices=["train", "evaluate"])
+    ap.add_argument("cmd", choices=["train", "evaluate", "profile"],
+                    help="profile: a few learned coarse steps on the 1M double dam break "
+                         "(a short run for a profiler's launch list)")
+    ap.add_argument("--steps", type=int, default=3, help="coarse steps of `profile`")
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--epochs", type=int, default=16)
     ap.add_argument("--batch", type=int, default=32768)
@@ -396,6 +399,19 @@ def main(argv=None) -> int:
         w = configs.dambreak_small(side=32, seed=9)
         print(json.dumps({"trained": model.info,
                           "one_step_32k": one_step_errors(model, w.xml, w.pos, w.vel)}))
+    elif a.cmd == "profile":
+        model = Model.load(a.model)
+        w = configs.dambreak_double()
+        with SPH(Scene.parse(w.xml).params) as s:
+            s.set_array(ARRAY_POS, w.pos)
+            s.set_array(ARRAY_VEL, w.vel)
+            s.update(20)
+            model.install(s)
+            learned_step(s, 1, SUBSTEPS, 1e9)  # allocations
+            s.update(2)
+            fb = learned_step(s, a.steps, SUBSTEPS, 1e9)
+            torch.cuda.synchronize()
+        print(json.dumps({"profile": "done", "coarse_steps": a.steps, "fallbacks": fb}))
     else:
         model = Model.load(a.model)
         w = configs.dambreak_double()
