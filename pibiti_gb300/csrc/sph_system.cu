@@ -495,7 +495,7 @@ __device__ __forceinline__ void force_item(const SceneDesc* __restrict__ sc, con
 }
 
 template <bool kMask, int kThreads, int kMinBlocks, bool kFeat>
-__global__ void __launch_bounds__(kThreads, kFeat ? kMinBlocks * 3 / 4 : kMinBlocks)
+__global__ void __launch_bounds__(kThreads, kFeat ? kMinBlocks * 7 / 8 : kMinBlocks)
 k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
         const float4* __restrict__ pos, const float4* __restrict__ vel,
         const float* __restrict__ dens, const float2* __restrict__ dp,
