@@ -78,10 +78,14 @@ __device__ __forceinline__ int scene_of(const uint32_t* __restrict__ off, int S,
 // Integrate particle i, find its cell and take a rank in it with one
 // atomicAdd per group of lanes sharing the cell.  Called by all 32 lanes
 // of a warp for consecutive i (i >= N: the lane takes part but does nothing).
-__device__ __forceinline__ void integrate_count_item(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S,
-                  uint32_t N, const float4* __restrict__ pos, const float4* __restrict__ vel,
-                  uint32_t* __restrict__ key, uint32_t* __restrict__ rank,
-                  uint32_t* __restrict__ count, uint32_t* __restrict__ flags, uint32_t i) {
+__device__ __forceinline__ void integrate_count_item(const SceneDesc* __restrict__ sc,
+                                                     const uint32_t* __restrict__ poff, int S,
+                                                     uint32_t N, const float4* __restrict__ pos,
+                                                     const float4* __restrict__ vel,
+                                                     uint32_t* __restrict__ key,
+                                                     uint32_t* __restrict__ rank,
+                                                     uint32_t* __restrict__ count,
+                                                     uint32_t* __restrict__ flags, uint32_t i) {
   const bool valid = i < N;
   uint32_t gcell = 0xffffffffu;
   if (valid) {
@@ -127,13 +131,19 @@ k_scatter_ids(uint32_t N, const uint32_t* __restrict__ key, const uint32_t* __re
 // original index, the order the reference's stable sort gives within a cell.
 constexpr uint32_t kLinearRank = 32;
 
-__device__ __forceinline__ void place_item(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
-        const float4* __restrict__ pos, const float4* __restrict__ vel,
-        const uint32_t* __restrict__ id, const uint32_t* __restrict__ key,
-        const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
-        const uint32_t* __restrict__ slot, float4* __restrict__ pos_out,
-        float4* __restrict__ vel_out, uint32_t* __restrict__ id_out,
-        float4* __restrict__ vel_start, uint32_t i) {
+__device__ __forceinline__ void place_item(const SceneDesc* __restrict__ sc,
+                                           const uint32_t* __restrict__ poff, int S, uint32_t N,
+                                           const float4* __restrict__ pos,
+                                           const float4* __restrict__ vel,
+                                           const uint32_t* __restrict__ id,
+                                           const uint32_t* __restrict__ key,
+                                           const uint32_t* __restrict__ start,
+                                           const uint32_t* __restrict__ count,
+                                           const uint32_t* __restrict__ slot,
+                                           float4* __restrict__ pos_out,
+                                           float4* __restrict__ vel_out,
+                                           uint32_t* __restrict__ id_out,
+                                           float4* __restrict__ vel_start, uint32_t i) {
   const uint32_t c = key[i], s0 = start[c], n = count[c], me = id[i];
   uint32_t r = 0;
   if (n <= kLinearRank) {
@@ -172,9 +182,11 @@ k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
 }
 
 // Launch shapes of the two walks: (threads per block, minimum resident
-// blocks per SM) pairs; sph_autotune picks one per handle by timing them on
-// the handle's own scenes.  Shape 1 (128, 4) is the default, the fastest on
-// GB300 for the 1M-particle dam break.
+// blocks per SM) pairs (64, 16), (128, 8), (256, 4), i.e. 64 registers per
+// thread (the featured force pass: 7/8 of those blocks, 72 registers);
+// sph_autotune picks one per handle by timing them on the handle's own
+// scenes.  Shape 1 (128 threads) is the default, the fastest on GB300 for
+// the 1M-particle dam break.
 constexpr int kWalkShapes = 3;
 constexpr int kWalkBlocks[kWalkShapes] = {64, 128, 256};
 constexpr int kDefaultShape = 1;
@@ -197,11 +209,16 @@ __device__ __forceinline__ float h2_out_of(const SimParams& p) {
 }
 
 template <bool kMask, bool kNC = true>
-__device__ __forceinline__ void density_item(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
-          const float4* __restrict__ pos, const uint32_t* __restrict__ start,
-          const uint32_t* __restrict__ count, float* __restrict__ dens_out,
-          float* __restrict__ pres_out, float2* __restrict__ dp_out,
-          unsigned long long* __restrict__ masks, uint32_t* __restrict__ flags, uint32_t i) {
+__device__ __forceinline__ void density_item(const SceneDesc* __restrict__ sc,
+                                             const uint32_t* __restrict__ poff, int S, uint32_t N,
+                                             const float4* __restrict__ pos,
+                                             const uint32_t* __restrict__ start,
+                                             const uint32_t* __restrict__ count,
+                                             float* __restrict__ dens_out,
+                                             float* __restrict__ pres_out,
+                                             float2* __restrict__ dp_out,
+                                             unsigned long long* __restrict__ masks,
+                                             uint32_t* __restrict__ flags, uint32_t i) {
   const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
   const SimParams& p = d.p;
   const float4 xi = pos[i];
@@ -300,11 +317,16 @@ struct FeatOut {
 };
 
 template <bool kMask, bool kFeat, bool kNC = true>
-__device__ __forceinline__ void force_item(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
-        const float4* __restrict__ pos, const float4* __restrict__ vel,
-        const float* __restrict__ dens, const float2* __restrict__ dp,
-        const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
-        const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out, FeatOut fo, uint32_t i) {
+__device__ __forceinline__ void force_item(const SceneDesc* __restrict__ sc,
+                                           const uint32_t* __restrict__ poff, int S, uint32_t N,
+                                           const float4* __restrict__ pos,
+                                           const float4* __restrict__ vel,
+                                           const float* __restrict__ dens,
+                                           const float2* __restrict__ dp,
+                                           const uint32_t* __restrict__ start,
+                                           const uint32_t* __restrict__ count,
+                                           const unsigned long long* __restrict__ masks,
+                                           float4* __restrict__ vel_out, FeatOut fo, uint32_t i) {
   const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
   const SimParams& p = d.p;
   const float4 xi = pos[i], vi = vel[i];
