@@ -92,3 +92,18 @@ def test_dam_break_frame(cuda):
     depth, thick, rgba = a
     assert np.all((depth >= 0) & (depth <= 1)) and np.isfinite(rgba).all()
     assert 0.05 < (depth < 1).mean() < 0.95
+
+
+def test_nothing_visible(cuda):
+    """Every particle behind the camera: no fragment, depth 1, background."""
+    torch = cuda
+    pos = np.ones((50, 4), np.float32)
+    pos[:, :3] = [0.5, 0.35, 30.0]
+    mv = look_at((0.5, 0.8, 2.0), (0.5, 0.35, 0.5))
+    pr = perspective(50.0, W / H, 0.1, 10.0)
+    with Renderer(W, H) as r:
+        d, t, c = (x.cpu().numpy() for x in r.frame(torch.from_numpy(pos).cuda(), mv, pr, radius=0.03,
+                                                     background=BG))
+        assert r.fragments == 0
+    assert np.all(d == 1) and np.all(t == 0)
+    np.testing.assert_allclose(c[..., :3], np.broadcast_to(np.array(BG, np.float32), (H, W, 3)))
