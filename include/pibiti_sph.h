@@ -245,6 +245,15 @@ int sph_mlp_packed_bytes(void);
 int sph_mlp_pack(const float* params, void* packed, void* stream);
 /* y[n][3] = MLP(x[n][16]); x is BF16 (uint16 bit patterns), y FP32. */
 int sph_mlp_forward(const void* packed, const uint16_t* x, uint32_t n, float* y, void* stream);
+/* The same forward pass on the 5th-generation tensor cores (tcgen05.mma with
+   the accumulators in tensor memory), with the same BF16 roundings: its
+   outputs equal sph_mlp_forward's.  x must be 16-byte aligned.  Its waits
+   for the tensor cores are bounded: a thread block whose wait runs out
+   writes NaN to the rows it did not finish and sets bit 0 of a status word
+   that sph_mlp_status reads and clears (synchronous).  The learned step
+   uses this pass; its density check treats NaN as a failed coarse step. */
+int sph_mlp_forward_tc(const void* packed, const uint16_t* x, uint32_t n, float* y, void* stream);
+int sph_mlp_status(uint32_t* status);
 /* One pass over n samples of the loss mean((y - target)^2) (over all 3n
    outputs): adds d loss / d params to grad[5443] and the loss to *loss
    (both FP32, zeroed by the caller). */

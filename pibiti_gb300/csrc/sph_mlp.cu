@@ -1,6 +1,9 @@
 // sph_mlp.cu -- the per-particle MLP corrector (16 -> 64 -> 64 -> 3, tanh)
-// on the tensor cores: BF16 operands, FP32 accumulation, mma.sync
-// m16n8k16 (one warp = 16 particles per tile).
+// on the tensor cores: BF16 operands, FP32 accumulation.  Training (forward
+// and backward) and one forward pass use mma.sync m16n8k16 (one warp = 16
+// particles per tile); the forward pass the learned step runs is a tcgen05
+// kernel with TMEM accumulators (k_forward_tc, at the end), bit-identical to
+// the mma.sync one.
 //
 // Parameters are kept in FP32 (training master copy) in one vector:
 //   W1[16][64] b1[64] W2[64][64] b2[64] W3[64][3] b3[3]   (5443 floats)
@@ -445,6 +448,305 @@ int sm_count() {
   }
   return n;
 }
+
+// ---- tcgen05 inference ------------------------------------------------------
+// The forward pass on the 5th-generation tensor cores: one CTA of 128
+// threads per 128-particle tile (grid-stride over tiles).  Each layer is a
+// tcgen05.mma (layer 1: 128x16 . 16x64, one instruction; layer 2: 128x64 .
+// 64x64 and layer 3: 128x64 . 64x16, four of K = 16 each) with BF16 operands
+// in shared memory (K-major core-matrix layout, no swizzle) and FP32
+// accumulators in one 64-column TMEM allocation that the three layers use in
+// turn.  Each warp reads its 32 rows (TMEM lanes 32w..32w+31) back with
+// tcgen05.ld; each layer's accumulators start from its bias (tcgen05.st),
+// tanh runs in registers and the BF16 activations go back to shared memory
+// as the next layer's A operand.  The input tile, the
+// layer-1 and the layer-2 activations share one buffer: each is dead once
+// the MMA that reads it has completed.  Only outputs 0..2 of layer 3 are
+// kept, so rows 3..15 of its B operand are don't-care: row 3 holds b3,
+// rows 4..7 the biases b1 and b2, rows 8..15 are the first bytes of W2^T.  That keeps a
+// CTA at 27.0 KB of shared memory, so 8 fit an SM with 8 x 64 = 512 TMEM
+// columns.  Thread 0 issues the MMAs and commits
+// them to one mbarrier; every wait on it is bounded (kTcSpins polls), after
+// which the CTA records an error (sph_mlp_status), writes NaN to the rows it
+// did not finish, and still frees its TMEM.
+namespace tcg {
+constexpr uint32_t kTcSpins = 1u << 22;
+// shared memory (bytes)
+constexpr uint32_t oH = 0;        // X 128 x 16, then H1 and H2 128 x 64 (BF16): 16 x 8 x 128 B
+constexpr uint32_t oW1 = 16384;   // W1^T 64 x 16 (N x K): 8 x 2 x 128 B
+constexpr uint32_t oW3 = 18432;   // W3^T rows 0..7 x 64: 8 x 128 B; rows 8..15 = oW2
+constexpr uint32_t oW2 = 19456;   // W2^T 64 x 64: 8 x 8 x 128 B
+constexpr uint32_t oBar = 27648;  // mbarrier (8 B)
+constexpr uint32_t oTmem = 27656; // TMEM base address written by tcgen05.alloc
+constexpr uint32_t kSmem = 27664;
+constexpr uint32_t kCols = 64;
+constexpr uint32_t kBlocksPerSm = 8;  // 8 x 64 = the 512 TMEM columns
+static_assert(kBlocksPerSm * kCols <= 512, "TMEM columns of the resident CTAs");
+static_assert(kBlocksPerSm * (kSmem + 1024) <= 233472, "shared memory of the resident CTAs");
+static_assert(oW3 + 1024 == oW2, "rows 8..15 of W3^T are read from W2^T");
+// bias value e of b1 (e < 64) or b2 (64 <= e < 128): K-core e / 16 of W3^T,
+// rows 4..7 (bytes 64..127), 16 floats per core
+__host__ __device__ constexpr uint32_t bias_off(uint32_t e) { return oW3 + (e >> 4) * 128u + 64u + (e & 15u) * 4u; }
+constexpr uint32_t oB3 = oW3 + 48;  // b3[3], 0: row 3 of K-core 0 of W3^T
+
+// Byte offset of element (r, k) (BF16) of a K-major operand made of 8-row x
+// 16-byte core matrices, `kc` cores along K: K-adjacent cores 128 B apart
+// (the descriptor's leading offset), row-adjacent cores 128 * kc B apart
+// (its stride offset).
+__host__ __device__ constexpr uint32_t core_off(uint32_t r, uint32_t k, uint32_t kc) {
+  return ((r >> 3) * kc + (k >> 3)) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// Shared-memory matrix descriptor: start address, leading and stride byte
+// offsets (all >> 4), descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc(uint32_t M, uint32_t N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+  for (uint32_t k = 0; k < kTcSpins; ++k)
+    if (mbar_try(bar, phase)) return true;
+  return false;
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// Orders this CTA's shared-memory stores and TMEM reads before what thread 0
+// issues next (the tensor core reads shared memory through the async proxy).
+__device__ __forceinline__ void sync_for_mma() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  fence_before();
+  __syncthreads();
+  fence_after();
+}
+__device__ __forceinline__ void umma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(id), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+// 32 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+               : "r"(taddr)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
+__device__ __forceinline__ void ld4(uint32_t taddr, float* v) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 4; ++k) v[k] = __uint_as_float(r[k]);
+}
+// Seeds this thread's TMEM lane with a layer's bias (columns 0..63), as
+// the mma.sync pass seeds its accumulators: the MMAs then add the products
+// to it, so both passes round the same sums.  `layer` 0 is b1, 1 is b2.
+__device__ __forceinline__ void st16(uint32_t taddr, const float* v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};" ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])), "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15])) : "memory");
+}
+__device__ __forceinline__ void seed_bias(uint32_t lane_base, const uint8_t* sm, uint32_t layer) {
+#pragma unroll 1
+  for (int q = 0; q < 4; ++q) {
+    float v[16];
+    const float4* b4 = reinterpret_cast<const float4*>(sm + bias_off(64u * layer + 16u * q));
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float4 b = b4[j];
+      v[4 * j] = b.x;
+      v[4 * j + 1] = b.y;
+      v[4 * j + 2] = b.z;
+      v[4 * j + 3] = b.w;
+    }
+    st16(lane_base + 16u * q, v);
+  }
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void seed_out_bias(uint32_t lane_base, const uint8_t* sm) {
+  const float4 b = *reinterpret_cast<const float4*>(sm + oB3);
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(lane_base),
+               "r"(__float_as_uint(b.x)), "r"(__float_as_uint(b.y)), "r"(__float_as_uint(b.z)),
+               "r"(__float_as_uint(b.w))
+               : "memory");
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+// tanh of this thread's row of the accumulators (64 columns, bias included)
+// as BF16 into row t of the activation buffer (core-matrix layout, 8
+// K-cores).
+__device__ __forceinline__ void activate(uint32_t lane_base, uint8_t* hbuf, uint32_t t) {
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    float v[32];
+    ld32(lane_base + 32u * half, v);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const uint32_t c0 = 32u * half + 16u * q;
+      uint32_t pk[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) pk[j] = tanh_pack2(v[16 * q + 2 * j], v[16 * q + 2 * j + 1]);
+      *reinterpret_cast<uint4*>(hbuf + core_off(t, c0, 8)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      *reinterpret_cast<uint4*>(hbuf + core_off(t, c0 + 8, 8)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+    }
+  }
+}
+}  // namespace tcg
+
+__device__ uint32_t g_tc_status;  // non-zero: a tcgen05 wait ran out (sph_mlp_status)
+
+__global__ void __launch_bounds__(128, tcg::kBlocksPerSm) k_forward_tc(const uint16_t* __restrict__ img,
+                                                                       const uint16_t* __restrict__ x,
+                                                                       uint32_t n, float* __restrict__ y) {
+  using namespace tcg;
+  extern __shared__ __align__(128) uint8_t sm[];
+  const uint32_t t = threadIdx.x, w = t >> 5;
+  const uint32_t sb = (uint32_t)__cvta_generic_to_shared(sm);
+  const uint32_t tiles = (n + 127) / 128;
+  // this thread's row of the next tile is fetched while the current one runs
+  uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0;
+  auto fetch = [&](uint32_t tile) {
+    const uint32_t r = tile * 128 + t;
+    c0 = c1 = make_uint4(0, 0, 0, 0);
+    if (tile < tiles && r < n) {
+      const uint4* src = reinterpret_cast<const uint4*>(x + (size_t)r * IN);
+      c0 = src[0];
+      c1 = src[1];
+    }
+  };
+  fetch(blockIdx.x);
+  // weights into the core-matrix layout (16-byte rows of 8 inputs; the
+  // image's row strides, 48 and 144 bytes, keep them aligned) and the biases
+  {
+    const uint32_t o = t >> 1, c = t & 1u;  // W1^T: 64 rows x 2 chunks
+    *reinterpret_cast<uint4*>(sm + oW1 + core_off(o, 8 * c, 2)) =
+        *reinterpret_cast<const uint4*>(img + oWT1 + o * S1 + 8 * c);
+  }
+  for (uint32_t e = t; e < 64 * 8; e += 128) {  // W2^T: 64 rows x 8 chunks
+    const uint32_t o = e >> 3, c = e & 7u;
+    *reinterpret_cast<uint4*>(sm + oW2 + core_off(o, 8 * c, 8)) =
+        *reinterpret_cast<const uint4*>(img + oWT2 + o * S2 + 8 * c);
+  }
+  const float* bimg = reinterpret_cast<const float*>(img + kHalves);  // b1 b2 b3
+  if (t < 3 * 8) {  // W3^T rows 0..2 x 8 chunks
+    const uint32_t o = t >> 3, c = t & 7u;
+    *reinterpret_cast<uint4*>(sm + oW3 + core_off(o, 8 * c, 8)) =
+        *reinterpret_cast<const uint4*>(img + oWT3 + o * S2 + 8 * c);
+  }
+  *reinterpret_cast<float*>(sm + bias_off(t)) = bimg[t];  // b1, b2 (128 values)
+  if (t < 4) reinterpret_cast<float*>(sm + oB3)[t] = t < OUT ? bimg[2 * HID + t] : 0.f;
+  if (t == 0) mbar_init(sb + oBar);
+  if (w == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sb + oTmem),
+                 "r"(kCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  sync_for_mma();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + oTmem);
+  const uint32_t lane_base = tmem + ((32u * w) << 16);
+  uint32_t phase = 0;
+  bool ok = true, pending = false;
+  // thread 0 issues, everyone waits (bounded); false when the wait ran out
+  auto run = [&](auto issue) {
+    if (t == 0) {
+      issue();
+      commit(sb + oBar);
+    }
+    pending = true;
+    ok = __syncthreads_and(mbar_wait(sb + oBar, phase));
+    if (!ok) return false;
+    pending = false;
+    phase ^= 1u;
+    fence_after();
+    return true;
+  };
+  uint32_t tile = blockIdx.x;
+  for (; tile < tiles; tile += gridDim.x) {
+    const uint32_t row = tile * 128 + t;
+    *reinterpret_cast<uint4*>(sm + oH + core_off(t, 0, 2)) = c0;
+    *reinterpret_cast<uint4*>(sm + oH + core_off(t, 8, 2)) = c1;
+    fetch(tile + gridDim.x);
+    seed_bias(lane_base, sm, 0);
+    sync_for_mma();
+    if (!run([&] { umma(tmem, sdesc(sb + oH, 128, 256), sdesc(sb + oW1, 128, 256), idesc(128, 64), 1u); }))
+      break;
+    activate(lane_base, sm + oH, t);  // H1
+    seed_bias(lane_base, sm, 1);
+    sync_for_mma();
+    if (!run([&] {
+          const uint64_t a = sdesc(sb + oH, 128, 1024), b = sdesc(sb + oW2, 128, 1024);
+#pragma unroll 1
+          for (uint32_t kk = 0; kk < 4; ++kk)  // K step of 16: 256 B, 16 in the address field
+            umma(tmem, a + 16u * kk, b + 16u * kk, idesc(128, 64), 1u);
+        }))
+      break;
+    activate(lane_base, sm + oH, t);  // H2
+    seed_out_bias(lane_base, sm);
+    sync_for_mma();
+    if (!run([&] {
+          const uint64_t a = sdesc(sb + oH, 128, 1024), b = sdesc(sb + oW3, 128, 1024);
+#pragma unroll 1
+          for (uint32_t kk = 0; kk < 4; ++kk)
+            umma(tmem, a + 16u * kk, b + 16u * kk, idesc(128, 16), 1u);
+        }))
+      break;
+    float o[4];
+    ld4(lane_base, o);
+    if (row < n) {
+      y[(size_t)row * OUT + 0] = o[0];
+      y[(size_t)row * OUT + 1] = o[1];
+      y[(size_t)row * OUT + 2] = o[2];
+    }
+    // this thread's next tcgen05.st comes after its own reads (wait::ld);
+    // the next tile's first sync_for_mma orders them all before its MMA
+  }
+  if (!ok) {
+    if (t == 0) atomicOr(&g_tc_status, 1u);
+    if (pending) __syncthreads_and(mbar_wait(sb + oBar, phase));  // the MMAs still in flight
+    // the rows this CTA did not finish become NaN, which a caller's
+    // finiteness check sees
+    for (; tile < tiles; tile += gridDim.x) {
+      const uint32_t row = tile * 128 + t;
+      if (row < n) y[(size_t)row * OUT + 0] = y[(size_t)row * OUT + 1] = y[(size_t)row * OUT + 2] = __int_as_float(0x7fc00000);
+    }
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (w == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+}
 }  // namespace
 
 extern "C" {
@@ -465,6 +767,23 @@ int sph_mlp_forward(const void* packed, const uint16_t* x, uint32_t n, float* y,
   const uint32_t blocks = (uint32_t)min((long long)(tiles + 3) / 4, (long long)sm_count() * 8);
   k_forward<<<blocks, 128, kPackedBytes, (cudaStream_t)stream>>>((const uint16_t*)packed, x, n, y);
   return cuda_check(cudaGetLastError(), "mlp_forward");
+}
+
+int sph_mlp_forward_tc(const void* packed, const uint16_t* x, uint32_t n, float* y, void* stream) {
+  if (!packed || (!x && n) || (!y && n)) return fail(SPH_ERR_ARG, "mlp_forward_tc: null pointer");
+  if ((uintptr_t)x & 15u) return fail(SPH_ERR_ARG, "mlp_forward_tc: features not 16-byte aligned");
+  if (n == 0) return SPH_OK;
+  const uint32_t tiles = (n + 127) / 128;
+  const uint32_t blocks = (uint32_t)min((long long)tiles, (long long)sm_count() * tcg::kBlocksPerSm);
+  k_forward_tc<<<blocks, 128, tcg::kSmem, (cudaStream_t)stream>>>((const uint16_t*)packed, x, n, y);
+  return cuda_check(cudaGetLastError(), "mlp_forward_tc");
+}
+
+int sph_mlp_status(uint32_t* status) {
+  if (!status) return fail(SPH_ERR_ARG, "mlp_status: null pointer");
+  const uint32_t zero = 0;
+  SPH_TRY(cuda_check(cudaMemcpyFromSymbol(status, g_tc_status, sizeof(uint32_t)), "mlp_status"));
+  return cuda_check(cudaMemcpyToSymbol(g_tc_status, &zero, sizeof(uint32_t)), "mlp_status");
 }
 
 int sph_mlp_train_pass(const void* packed, const uint16_t* x, const float* target, uint32_t n,

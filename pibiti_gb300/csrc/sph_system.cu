@@ -1700,7 +1700,7 @@ int sph_learned_step(SphSystem* s, uint32_t coarse_steps, uint32_t substeps, flo
     // the velocity (overwritten by the force pass) needs a checkpoint.
     SPH_CUDA(cudaMemcpyAsync(s->bk_vel, s->vel[s->cv], sizeof(float4) * s->N, cudaMemcpyDeviceToDevice, st), "checkpoint");
     SPH_TRY(enqueue_step(s, st, nullptr, &o));
-    SPH_TRY(sph_mlp_forward(s->mlp_img, s->feat, s->N, s->mlp_y, st));
+    SPH_TRY(sph_mlp_forward_tc(s->mlp_img, s->feat, s->N, s->mlp_y, st));
     k_apply_correction<<<grid_for(s->N, kBlock), kBlock, 0, st>>>(
         s->d_coarse, s->d_poff, s->S, s->N, s->mlp_y, s->mlp_aux + 32, drift, jerk, s->vstart,
         s->vel[1 - s->cv], s->id[s->cp], s->hist, s->hist_valid, s->pos[s->cp], s->vel[s->cv]);

@@ -60,6 +60,47 @@ def test_forward(cuda, n):
     np.testing.assert_allclose(y.cpu().numpy(), ref, rtol=0, atol=1e-2 * scale)
 
 
+@pytest.mark.parametrize("n", [1, 37, 128, 4096, 100_003])
+def test_forward_tc(cuda, n):
+    """The tcgen05 forward pass: against the oracle with the same bound as
+    the mma.sync pass, and bit-identical to the mma.sync pass (both seed the
+    accumulators with the bias, add the K = 16 products in the same order and
+    round to BF16 at the same places)."""
+    torch = cuda
+    _l, L = _lib()
+    rng = np.random.default_rng(100 + n)
+    params = omlp.init(4)
+    params[1024:1088] = rng.normal(0, 0.1, 64)
+    params[1088 + 4096:1088 + 4096 + 64] = rng.normal(0, 0.1, 64)
+    params[5440:5443] = rng.normal(0, 0.1, 3)
+    x = rng.normal(0, 1, size=(n, 16)).astype(np.float32)
+    _, img = _pack(torch, params)
+    xd = _x(torch, x)
+    y_tc = torch.full((n, 3), float("nan"), dtype=torch.float32, device="cuda")
+    y_mma = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
+    _l.check(L.sph_mlp_forward_tc(_p(img), _p(xd), n, _p(y_tc), None))
+    _l.check(L.sph_mlp_forward(_p(img), _p(xd), n, _p(y_mma), None))
+    status = ctypes.c_uint32(7)
+    _l.check(L.sph_mlp_status(ctypes.byref(status)))
+    assert status.value == 0
+    ref, _ = omlp.forward(params, x)
+    scale = max(np.abs(ref).max(), 1e-3)
+    a, b = y_tc.cpu().numpy(), y_mma.cpu().numpy()
+    np.testing.assert_allclose(a, ref, rtol=0, atol=1e-2 * scale)
+    np.testing.assert_array_equal(a, b)
+
+
+def test_forward_tc_arguments(cuda):
+    torch = cuda
+    _l, L = _lib()
+    _, img = _pack(torch, omlp.init(1))
+    x = torch.zeros(64 * 16 + 8, dtype=torch.int16, device="cuda")
+    y = torch.zeros((64, 3), dtype=torch.float32, device="cuda")
+    misaligned = ctypes.c_void_p(x.data_ptr() + 2)
+    assert L.sph_mlp_forward_tc(_p(img), misaligned, 64, _p(y), None) != 0
+    assert L.sph_mlp_forward_tc(_p(img), _p(x), 0, _p(y), None) == 0
+
+
 @pytest.mark.parametrize("n", [64, 1000, 50_000])
 def test_gradients(cuda, n):
     torch = cuda
