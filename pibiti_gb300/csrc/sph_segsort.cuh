@@ -1,21 +1,26 @@
-// sph_segsort.cuh -- sorting many independent segments of uint32 keys in
-// place (segment k: data[start[k], start[k] + count[k])), used for the ids
-// of crowded grid cells and for the per-pixel fragment lists of the
-// renderer.  Three kernels:
+// sph_segsort.cuh -- sorting many independent segments of uint32 keys
+// (segment k: data[start[k], start[k] + count[k])), used for the ids of
+// crowded grid cells and for the per-pixel fragment lists of the renderer.
+// Three kernels:
 //   k_find_cells      segments longer than `min_sort` go to `list` (up to
 //                     kWarpSortMax) or `big_list`, one atomic per warp and list
-//   k_sort_cells      one warp per listed segment: bitonic in shared memory
+//   k_sort_cells      one warp per listed segment: bitonic in registers
+//                     (warp_sort_segment)
 //   k_sort_big_cells  one block per big segment: bitonic in shared memory up
 //                     to kBlockSortMax keys, beyond that in `scratch`
 //                     (2 words per key, segment k at 2 * start[k], so the
 //                     padded segments never overlap)
+// The sorted keys go back in place, or, when the keys are distinct particle
+// ids and `dest_of` is given, dest_of[key] = the key's sorted position
+// (start[k] + rank) is written instead, which is all the cell placement
+// needs.
 #pragma once
 #include <cstdint>
 
 namespace sph {
 namespace {
 
-constexpr uint32_t kWarpSortMax = 1024;   // sorted by one warp in shared memory
+constexpr uint32_t kWarpSortMax = 1024;   // sorted by one warp in registers
 constexpr uint32_t kBlockSortMax = 16384; // sorted by one block in shared memory
 constexpr int kSortWarps = 4;
 constexpr int kBigThreads = 1024;
@@ -25,14 +30,16 @@ __device__ __forceinline__ uint32_t pow2_at_least(uint32_t n) {
 }
 
 // Bitonic sort of buf[0, m) (m a power of two) by `lanes` cooperating
-// threads with index `me`; `sync` orders the stages.
+// threads with index `me`; `sync` orders the stages.  Compare-exchange t of
+// a stage pairs i = 2 * stride * (t / stride) + t % stride with i + stride;
+// stride is a power of two, so i = 2t - (t & (stride - 1)).
 template <class Sync>
 __device__ __forceinline__ void bitonic(uint32_t* buf, uint32_t m, uint32_t me, uint32_t lanes,
                                         Sync sync) {
   for (uint32_t size = 2; size <= m; size <<= 1)
     for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
       for (uint32_t t = me; t < (m >> 1); t += lanes) {
-        const uint32_t i = 2 * stride * (t / stride) + (t % stride), j = i + stride;
+        const uint32_t i = 2 * t - (t & (stride - 1)), j = i + stride;
         const bool up = (i & size) == 0;
         const uint32_t a = buf[i], b = buf[j];
         if ((a > b) == up) {
@@ -42,6 +49,112 @@ __device__ __forceinline__ void bitonic(uint32_t* buf, uint32_t m, uint32_t me, 
       }
       sync();
     }
+}
+
+// One stage of stride ST < E (within each lane) and one of stride st >= E
+// (lane mask st / E, by shuffles).  The stage loops stay rolled so that the
+// kernel's code stays small: only the E positions of a lane are unrolled,
+// which keeps v[] in registers.
+template <int E, uint32_t ST>
+__device__ __forceinline__ void stage_in_lane(uint32_t (&v)[E], uint32_t size, uint32_t lane) {
+#pragma unroll
+  for (uint32_t e = 0; e < (uint32_t)E; ++e) {
+    if (e & ST) continue;
+    const bool asc = ((lane * E + e) & size) == 0;
+    const uint32_t a = v[e], b = v[e | ST];
+    v[e] = asc ? min(a, b) : max(a, b);
+    v[e | ST] = asc ? max(a, b) : min(a, b);
+  }
+}
+template <int E>
+__device__ __forceinline__ void stage_across(uint32_t (&v)[E], uint32_t size, uint32_t lm, uint32_t lane) {
+  const bool lower = (lane & lm) == 0;
+#pragma unroll
+  for (uint32_t e = 0; e < (uint32_t)E; ++e) {
+    const uint32_t o = __shfl_xor_sync(0xffffffffu, v[e], lm);
+    const bool asc = ((lane * E + e) & size) == 0;
+    v[e] = asc == lower ? min(v[e], o) : max(v[e], o);
+  }
+}
+
+// Bitonic sort of the 32 * E keys a warp holds in registers, v[e] of lane
+// `lane` at network position k = lane * E + e (the keys may be loaded in
+// any order: the network sorts whatever it is given, and after it the key
+// of rank k is at position k).  The partner of position k in a stage of
+// stride st is k ^ st: v[e ^ st] of the same lane when st < E, the same
+// e of lane lane ^ (st / E) otherwise.  Ascending where (k & size) == 0;
+// the lower position of a pair keeps the minimum when ascending.  With
+// E = 32 the 40 stages of stride < 32 are compare-exchanges in registers
+// and only 15 are shuffles.
+template <int E>
+__device__ __forceinline__ void warp_bitonic(uint32_t (&v)[E], uint32_t lane) {
+  constexpr uint32_t M = 32u * E;
+#pragma unroll 1
+  for (uint32_t size = 2; size <= M; size <<= 1) {
+#pragma unroll 1
+    for (uint32_t st = size >> 1; st > 0; st >>= 1) {
+      if (st >= (uint32_t)E) {
+        stage_across<E>(v, size, st / E, lane);
+      } else {
+        switch (st) {
+          case 1: if constexpr (E > 1) stage_in_lane<E, 1>(v, size, lane); break;
+          case 2: if constexpr (E > 2) stage_in_lane<E, 2>(v, size, lane); break;
+          case 4: if constexpr (E > 4) stage_in_lane<E, 4>(v, size, lane); break;
+          case 8: if constexpr (E > 8) stage_in_lane<E, 8>(v, size, lane); break;
+          default: if constexpr (E > 16) stage_in_lane<E, 16>(v, size, lane); break;
+        }
+      }
+    }
+  }
+}
+
+template <int E>
+__device__ __forceinline__ void warp_sort_n(uint32_t* __restrict__ data, uint32_t s0, uint32_t n,
+                                            uint32_t lane, uint32_t* __restrict__ dest_of) {
+  uint32_t v[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {  // coalesced loads; padding sorts last
+    const uint32_t k = 32u * e + lane;
+    v[e] = k < n ? data[s0 + k] : 0xffffffffu;
+  }
+  warp_bitonic<E>(v, lane);
+  if (!dest_of) __syncwarp();  // every lane has read its keys before any is written back
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const uint32_t k = lane * E + e;  // rank of v[e]
+    if (k < n) {
+      if (dest_of) dest_of[v[e]] = s0 + k;
+      else data[s0 + k] = v[e];
+    }
+  }
+}
+
+// One warp sorts segment data[s0, s0 + n), n <= kWarpSortMax.
+__device__ __forceinline__ void warp_sort_segment(uint32_t* __restrict__ data, uint32_t s0, uint32_t n,
+                                                  uint32_t lane, uint32_t* __restrict__ dest_of) {
+  if (n <= 32) warp_sort_n<1>(data, s0, n, lane, dest_of);
+  else if (n <= 64) warp_sort_n<2>(data, s0, n, lane, dest_of);
+  else if (n <= 128) warp_sort_n<4>(data, s0, n, lane, dest_of);
+  else if (n <= 256) warp_sort_n<8>(data, s0, n, lane, dest_of);
+  else if (n <= 512) warp_sort_n<16>(data, s0, n, lane, dest_of);
+  else warp_sort_n<32>(data, s0, n, lane, dest_of);
+}
+static_assert(kWarpSortMax == 32 * 32, "warp_sort_segment covers up to 32 keys per lane");
+
+// The same with the keys in shared memory (buf: kWarpSortMax words of this
+// warp), for kernels that cannot spare the registers.
+__device__ __forceinline__ void warp_sort_segment_smem(uint32_t* __restrict__ data, uint32_t s0, uint32_t n,
+                                                       uint32_t lane, uint32_t* __restrict__ dest_of,
+                                                       uint32_t* buf) {
+  const uint32_t m = pow2_at_least(n);
+  for (uint32_t k = lane; k < m; k += 32) buf[k] = k < n ? data[s0 + k] : 0xffffffffu;
+  __syncwarp();
+  bitonic(buf, m, lane, 32, [] { __syncwarp(); });
+  for (uint32_t k = lane; k < n; k += 32) {
+    if (dest_of) dest_of[buf[k]] = s0 + k;
+    else data[s0 + k] = buf[k];
+  }
+  __syncwarp();
 }
 
 __global__ void k_find_cells(uint32_t C, const uint32_t* __restrict__ count, uint32_t min_sort,
@@ -67,25 +180,20 @@ __global__ void k_find_cells(uint32_t C, const uint32_t* __restrict__ count, uin
 __global__ void __launch_bounds__(kSortWarps * 32)
 k_sort_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
              uint32_t* __restrict__ slot, const uint32_t* __restrict__ list,
-             const uint32_t* __restrict__ counters) {
-  __shared__ uint32_t buf[kSortWarps][kWarpSortMax];
+             const uint32_t* __restrict__ counters, uint32_t* __restrict__ dest_of = nullptr) {
   const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t nl = counters[0];
   for (uint32_t q = blockIdx.x * kSortWarps + w; q < nl; q += gridDim.x * kSortWarps) {
-    const uint32_t c = list[q], n = count[c], s0 = start[c], m = pow2_at_least(n);
-    uint32_t* b = buf[w];
-    for (uint32_t k = lane; k < m; k += 32) b[k] = k < n ? slot[s0 + k] : 0xffffffffu;
-    __syncwarp();
-    bitonic(b, m, lane, 32, [] { __syncwarp(); });
-    for (uint32_t k = lane; k < n; k += 32) slot[s0 + k] = b[k];
-    __syncwarp();
+    const uint32_t c = list[q];
+    warp_sort_segment(slot, start[c], count[c], lane, dest_of);
   }
 }
 
 __global__ void __launch_bounds__(kBigThreads)
 k_sort_big_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
                  uint32_t* __restrict__ slot, const uint32_t* __restrict__ big_list,
-                 const uint32_t* __restrict__ big_count, uint32_t* __restrict__ scratch) {
+                 const uint32_t* __restrict__ big_count, uint32_t* __restrict__ scratch,
+                 uint32_t* __restrict__ dest_of = nullptr) {
   extern __shared__ uint32_t sbuf[];
   const uint32_t nbig = *big_count;
   for (uint32_t q = blockIdx.x; q < nbig; q += gridDim.x) {
@@ -100,7 +208,10 @@ k_sort_big_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict_
         __threadfence_block();
         __syncthreads();
       });
-    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) slot[s0 + k] = b[k];
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+      if (dest_of) dest_of[b[k]] = s0 + k;
+      else slot[s0 + k] = b[k];
+    }
     __syncthreads();
   }
 }

@@ -126,9 +126,10 @@ k_scatter_ids(uint32_t N, const uint32_t* __restrict__ key, const uint32_t* __re
 }
 
 // Cells with more than kLinearRank particles get their id segment of
-// `slot` sorted (sph_segsort.cuh) so that k_place finds a particle's rank
-// by binary search; smaller cells are counted linearly.  Sorting is by
-// original index, the order the reference's stable sort gives within a cell.
+// `slot` sorted (sph_segsort.cuh), which writes each id's sorted position to
+// dest_of[id] for k_place; in smaller cells k_place counts the smaller ids
+// linearly.  Sorting is by original index, the order the reference's stable
+// sort gives within a cell.
 constexpr uint32_t kLinearRank = 32;
 
 __device__ __forceinline__ void place_item(const SceneDesc* __restrict__ sc,
@@ -140,23 +141,20 @@ __device__ __forceinline__ void place_item(const SceneDesc* __restrict__ sc,
                                            const uint32_t* __restrict__ start,
                                            const uint32_t* __restrict__ count,
                                            const uint32_t* __restrict__ slot,
+                                           const uint32_t* __restrict__ dest_of,
                                            float4* __restrict__ pos_out,
                                            float4* __restrict__ vel_out,
                                            uint32_t* __restrict__ id_out,
                                            float4* __restrict__ vel_start, uint32_t i) {
   const uint32_t c = key[i], s0 = start[c], n = count[c], me = id[i];
-  uint32_t r = 0;
+  uint32_t dest;
   if (n <= kLinearRank) {
+    uint32_t r = 0;
     for (uint32_t j = s0; j < s0 + n; ++j) r += slot[j] < me;
-  } else {  // sorted segment: number of smaller ids by binary search
-    uint32_t lo = 0, hi = n;
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (slot[s0 + mid] < me) lo = mid + 1; else hi = mid;
-    }
-    r = lo;
+    dest = s0 + r;
+  } else {
+    dest = dest_of[me];  // written by the cell's sort
   }
-  const uint32_t dest = s0 + r;
   const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
   const float4 x4 = pos[i], v4 = vel[i];
   float3 x = make_float3(x4.x, x4.y, x4.z), v = make_float3(v4.x, v4.y, v4.z);
@@ -172,12 +170,12 @@ k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
         const float4* __restrict__ pos, const float4* __restrict__ vel,
         const uint32_t* __restrict__ id, const uint32_t* __restrict__ key,
         const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
-        const uint32_t* __restrict__ slot, float4* __restrict__ pos_out,
-        float4* __restrict__ vel_out, uint32_t* __restrict__ id_out,
+        const uint32_t* __restrict__ slot, const uint32_t* __restrict__ dest_of,
+        float4* __restrict__ pos_out, float4* __restrict__ vel_out, uint32_t* __restrict__ id_out,
         float4* __restrict__ vel_start = nullptr) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
-  place_item(sc, poff, S, N, pos, vel, id, key, start, count, slot, pos_out, vel_out, id_out,
+  place_item(sc, poff, S, N, pos, vel, id, key, start, count, slot, dest_of, pos_out, vel_out, id_out,
              vel_start, i);
 }
 
@@ -786,7 +784,7 @@ struct PersistArgs {
   uint32_t N, C;
   float4 *pos0, *pos1, *vel0, *vel1;
   uint32_t *id0, *id1;
-  uint32_t *key, *rank, *slot, *count, *start, *tsum;
+  uint32_t *key, *rank, *slot, *dest, *count, *start, *tsum;
   float *dens, *pres;
   float2* dp;
   unsigned long long* masks;
@@ -857,10 +855,10 @@ __device__ __forceinline__ uint32_t p_block_scan(uint32_t v, uint32_t* wtot, uin
 }
 
 __global__ void __launch_bounds__(kPThreads, 4) k_persistent(PersistArgs a) {
-  extern __shared__ uint32_t psm[];  // kPWarps x kWarpSortMax words
+  extern __shared__ uint32_t psm[];  // kPBlockSortMax words: a warp's or a block's cell ids
   __shared__ uint32_t wtot[32];
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
-  const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const uint32_t lane = threadIdx.x & 31;
   const uint32_t gwarp = tid >> 5, nwarps = nthr >> 5;
   const uint32_t tiles = (a.C + kPTile - 1) / kPTile;
   float4* vel_v = a.cv ? a.vel1 : a.vel0;
@@ -937,14 +935,10 @@ __global__ void __launch_bounds__(kPThreads, 4) k_persistent(PersistArgs a) {
     // sort: a warp per listed cell, then a block per big cell
     {
       const uint32_t nl = *((volatile uint32_t*)a.sort_counters);
-      uint32_t* b = psm + wib * kWarpSortMax;
       for (uint32_t q = gwarp; q < nl; q += nwarps) {
-        const uint32_t c = a.sort_list[q], n = a.count[c], s0 = a.start[c], m = pow2_at_least(n);
-        for (uint32_t k = lane; k < m; k += 32) b[k] = k < n ? a.slot[s0 + k] : 0xffffffffu;
-        __syncwarp();
-        bitonic(b, m, lane, 32, [] { __syncwarp(); });
-        for (uint32_t k = lane; k < n; k += 32) a.slot[s0 + k] = b[k];
-        __syncwarp();
+        const uint32_t c = a.sort_list[q];
+        warp_sort_segment_smem(a.slot, a.start[c], a.count[c], lane, a.dest,
+                               psm + (threadIdx.x >> 5) * kWarpSortMax);
       }
       __syncthreads();
       const uint32_t nb = *((volatile uint32_t*)(a.sort_counters + 1));
@@ -960,14 +954,14 @@ __global__ void __launch_bounds__(kPThreads, 4) k_persistent(PersistArgs a) {
             __threadfence_block();
             __syncthreads();
           });
-        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) a.slot[s0 + k] = bb[k];
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) a.dest[bb[k]] = s0 + k;
         __syncthreads();
       }
     }
     if (!grid_barrier(a.bar, a.flags)) return;
     for (uint32_t i = tid; i < a.N; i += nthr)
-      place_item(a.sc, a.poff, a.S, a.N, pa, vel_v, ia, a.key, a.start, a.count, a.slot, pb, vel_o, ib,
-                 nullptr, i);
+      place_item(a.sc, a.poff, a.S, a.N, pa, vel_v, ia, a.key, a.start, a.count, a.slot, a.dest, pb, vel_o,
+                 ib, nullptr, i);
     if (!grid_barrier(a.bar, a.flags)) return;
     for (uint32_t i = tid; i < a.N; i += nthr)
       density_item<true, false>(a.sc, a.poff, a.S, a.N, pb, a.start, a.count, a.dens, a.pres, a.dp, a.masks,
@@ -999,6 +993,7 @@ struct SphSystem {
   float4* vel[2] = {nullptr, nullptr};
   uint32_t* id[2] = {nullptr, nullptr};
   uint32_t *key = nullptr, *rank = nullptr, *slot = nullptr;
+  uint32_t* dest = nullptr;  // sorted position of each id of a crowded cell
   uint32_t *big_list = nullptr, *sort_scratch = nullptr;
   uint32_t *sort_list = nullptr, *sort_counters = nullptr;  // counters: list, big_list sizes
   unsigned big_blocks = 1, sort_blocks = 1;
@@ -1154,12 +1149,12 @@ int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr,
   k_find_cells<<<grid_for(s->C, kBlock), kBlock, 0, st>>>(s->C, s->count, kLinearRank,
                                                           s->sort_list, s->sort_counters, s->big_list);
   k_sort_cells<<<s->sort_blocks, kSortWarps * 32, 0, st>>>(s->start, s->count, s->slot,
-                                                           s->sort_list, s->sort_counters);
+                                                           s->sort_list, s->sort_counters, s->dest);
   k_sort_big_cells<<<s->big_blocks, kBigThreads, kBlockSortMax * sizeof(uint32_t), st>>>(
-      s->start, s->count, s->slot, s->big_list, s->sort_counters + 1, s->sort_scratch);
+      s->start, s->count, s->slot, s->big_list, s->sort_counters + 1, s->sort_scratch, s->dest);
   mark();
   k_place<<<gN, kBlock, 0, st>>>(sc, s->d_poff, s->S, s->N, s->pos[a], s->vel[v], s->id[a],
-                                 s->key, s->start, s->count, s->slot, s->pos[b], s->vel[1 - v],
+                                 s->key, s->start, s->count, s->slot, s->dest, s->pos[b], s->vel[1 - v],
                                  s->id[b], o.vel_start);
   mark();
   if (s->masks)
@@ -1199,7 +1194,7 @@ int build_graph(SphSystem* s) {
 void free_all(SphSystem* s) {
   drop_graphs(s);
   void* bufs[] = {s->d_scenes, s->d_poff, s->d_coff, s->pos[0], s->pos[1], s->vel[0], s->vel[1],
-                  s->id[0], s->id[1], s->key, s->rank, s->slot, s->count, s->start, s->scan_tmp,
+                  s->id[0], s->id[1], s->key, s->rank, s->slot, s->dest, s->count, s->start, s->scan_tmp,
                   s->dens, s->pres, s->dp, s->masks, s->flags, s->stats, s->staging, s->d_coarse,
                   s->mlp_img, s->mlp_aux, s->feat, s->mlp_y, s->bk_vel, s->vstart, s->hist, s->ptsum, s->pbar,
                   s->big_list, s->sort_counters, s->sort_list, s->sort_scratch};
@@ -1253,6 +1248,7 @@ int create(const SimParams* scenes, uint32_t count, SphSystem** out) {
   ALLOC(s->key, n, "cell keys");
   ALLOC(s->rank, n, "cell ranks");
   ALLOC(s->slot, n, "cell slots");
+  ALLOC(s->dest, n, "sorted positions");
   ALLOC(s->big_list, n / (kWarpSortMax + 1) + 1, "crowded-cell list");
   ALLOC(s->sort_list, n / (kLinearRank + 1) + 1, "cell sort list");
   ALLOC(s->sort_counters, 2, "cell sort list sizes");
@@ -1430,6 +1426,7 @@ static int persistent_steps(SphSystem* s, uint32_t steps) {
   a.key = s->key;
   a.rank = s->rank;
   a.slot = s->slot;
+  a.dest = s->dest;
   a.count = s->count;
   a.start = s->start;
   a.tsum = s->ptsum;
