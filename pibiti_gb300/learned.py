@@ -353,6 +353,42 @@ def rollout(model: Model, xml: str, pos, vel, fine_steps: int, substeps: int = S
     return out
 
 
+def mlp_bench(model: Model, rows: int, reps: int = 20, seed: int = 0) -> dict:
+    """The mma.sync and the tcgen05 forward pass (sph_mlp_forward,
+    sph_mlp_forward_tc) on `rows` standard-normal BF16 feature rows with the
+    model's weights: median CUDA-event time of `reps` launches each (L2
+    flushed before each), and whether the outputs are bit-identical."""
+    import torch
+    L = _lib.lib()
+    prm = torch.from_numpy(model.params).cuda()
+    img = torch.zeros(L.sph_mlp_packed_bytes(), dtype=torch.uint8, device="cuda")
+    _lib.check(L.sph_mlp_pack(_p(prm), _p(img), None))
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    x = torch.randn((rows, 16), generator=g, device="cuda").to(torch.bfloat16).view(torch.int16)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    out = {"rows": rows}
+    ys = {}
+    for name, fn in (("mma_sync", L.sph_mlp_forward), ("tcgen05", L.sph_mlp_forward_tc)):
+        y = torch.zeros((rows, 3), dtype=torch.float32, device="cuda")
+        _lib.check(fn(_p(img), _p(x), rows, _p(y), None))
+        ts = []
+        for _ in range(reps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _lib.check(fn(_p(img), _p(x), rows, _p(y), None))
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e3)
+        out[f"{name}_us"] = sorted(ts)[len(ts) // 2]
+        ys[name] = y
+    status = ctypes.c_uint32(0)
+    _lib.check(L.sph_mlp_status(ctypes.byref(status)))
+    out["identical"] = bool(torch.equal(ys["mma_sync"], ys["tcgen05"]))
+    out["tc_status"] = status.value
+    return out
+
+
 def main(argv=None) -> int:
     """python -m pibiti_gb300.learned train|evaluate [--scenes S] ..."""
     import argparse
@@ -361,10 +397,13 @@ def main(argv=None) -> int:
     import torch
     from . import configs
     ap = argparse.ArgumentParser()
-    ap.add_argument("cmd", choices=["train", "evaluate", "profile"],
+    ap.add_argument("cmd", choices=["train", "evaluate", "profile", "mlp-bench"],
                     help="profile: a few learned coarse steps on the 1M double dam break "
-                         "(a short run for a profiler's launch list)")
+                         "(a short run for a profiler's launch list); mlp-bench: the two "
+                         "forward kernels on --rows standard-normal feature rows")
     ap.add_argument("--steps", type=int, default=3, help="coarse steps of `profile`")
+    ap.add_argument("--rows", type=int, default=1 << 20, help="rows of `mlp-bench`")
+    ap.add_argument("--reps", type=int, default=20, help="timed launches of `mlp-bench`")
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--epochs", type=int, default=16)
     ap.add_argument("--batch", type=int, default=32768)
@@ -412,6 +451,8 @@ def main(argv=None) -> int:
             fb = learned_step(s, a.steps, SUBSTEPS, 1e9)
             torch.cuda.synchronize()
         print(json.dumps({"profile": "done", "coarse_steps": a.steps, "fallbacks": fb}))
+    elif a.cmd == "mlp-bench":
+        print(json.dumps(mlp_bench(Model.load(a.model), a.rows, a.reps)))
     else:
         model = Model.load(a.model)
         w = configs.dambreak_double()
