@@ -51,6 +51,28 @@ def test_fallback_reproduces_fine_steps(cuda):
         np.testing.assert_array_equal(a.get_array(ARRAY_VEL), b.get_array(ARRAY_VEL))
 
 
+def test_nonfinite_corrections_fall_back(cuda):
+    """NaN network outputs (here from NaN output biases; the tcgen05 forward
+    pass also writes NaN rows when a wait for the tensor cores runs out) make
+    the corrected state non-finite: with a density tolerance that never
+    fails, the finiteness check alone rejects every coarse step, and the
+    result equals the plain steps bit for bit."""
+    w = configs.dambreak_small(side=12)
+    params = np.zeros(5443, np.float32)
+    params[5440:5443] = np.nan  # b3
+    model = learned.Model(params, np.zeros(16, np.float32), np.ones(16, np.float32),
+                          np.ones(3, np.float32), {})
+    with _sys(w.xml, w.pos, w.vel) as a, _sys(w.xml, w.pos, w.vel) as b:
+        a.update(1)
+        b.update(1)
+        model.install(a)
+        fb = learned.learned_step(a, 3, 4, tol=1e9)
+        b.update(12)
+        assert fb == 3
+        np.testing.assert_array_equal(a.get_array(ARRAY_POS), b.get_array(ARRAY_POS))
+        np.testing.assert_array_equal(a.get_array(ARRAY_VEL), b.get_array(ARRAY_VEL))
+
+
 def test_training_lowers_loss(cuda):
     """The project's own forward/backward kernels and Adam, run on a small
     ensemble, lower the training loss."""
