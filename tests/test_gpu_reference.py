@@ -1,0 +1,114 @@
+"""The reference's own CUDA kernels on the GPU (oracle/ref_gpu.py: its
+System.cu and radixsort_kernel.cu compiled for sm_103a, launched as its
+wrappers launch them) against the fused step, from the same state.
+
+Bit for bit: the positions after integrate, the sorted (hash, index) pairs
+and cellStart.  Density (sorted order) and the new velocities within 1e-5
+relative (velocities: of their largest magnitude): the reference sums
+density with pow(c, 3) and contracts nothing (built with --fmad=false, like
+its host build that pins the oracle), the fused step with FMAs in the
+places the oracle has them.
+
+The last test times the reference's step (nvcc's default flags, every
+wrapper synchronising as the reference's do) against the fused step on the
+1,048,576-particle double dam break and prints one JSON line.
+"""
+import json
+import time
+
+import numpy as np
+import pytest
+
+from oracle import ref_gpu
+from pibiti_gb300 import configs
+from pibiti_gb300.sph import ARRAY_POS, ARRAY_VEL, SPH, Scene
+
+pytestmark = pytest.mark.gpu
+
+DENS_RTOL = 1e-5
+VEL_RTOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def ref(cuda):
+    if not ref_gpu.available():
+        pytest.skip("the reference's kernels were not compiled to PTX (reference tree absent at build)")
+    return ref_gpu
+
+
+def _state(w, warm):
+    p = Scene.parse(w.xml).params
+    with SPH(p) as s:
+        s.set_array(ARRAY_POS, w.pos)
+        s.set_array(ARRAY_VEL, w.vel)
+        s.update(warm)
+        return p, s.get_array(ARRAY_POS), s.get_array(ARRAY_VEL)
+
+
+def _compare(p, pos, vel, ref):
+    r = ref.RefStep(p, pos, vel)
+    r.update(1)
+    got = r.results()
+    with SPH(p) as s:
+        s.set_array(ARRAY_POS, pos)
+        s.set_array(ARRAY_VEL, vel)
+        s.update(1)
+        sh, cs, ce = s.cells()
+        dens, _ = s.fields()
+        opos, ovel = s.get_array(ARRAY_POS), s.get_array(ARRAY_VEL)
+    np.testing.assert_array_equal(opos, got["pos"])
+    np.testing.assert_array_equal(sh, got["sorted"])
+    nz = ce > cs
+    np.testing.assert_array_equal(cs[nz], got["cell_start"][nz])
+    assert np.all(got["cell_start"][~nz] == 0xFFFFFFFF)
+    np.testing.assert_allclose(dens, got["density"], rtol=DENS_RTOL, atol=1e-3)
+    scale = np.abs(got["vel"][:, :3]).max()
+    np.testing.assert_allclose(ovel[:, :3], got["vel"][:, :3], rtol=0, atol=VEL_RTOL * scale)
+    return got
+
+
+def test_single_dam_break_32k(ref):
+    """32,768 particles (a 32^3 lattice at spacing 0.5h in a unit box),
+    after 30 steps."""
+    w = configs.dambreak_small(side=32)
+    p, pos, vel = _state(w, 30)
+    got = _compare(p, pos, vel, ref)
+    assert np.count_nonzero(got["cell_start"] != 0xFFFFFFFF) > 100
+
+
+def test_double_dam_break_1m(ref):
+    """The 1,048,576-particle double dam break after 20 steps (376,200
+    cells: 32-bit keys, four radix passes)."""
+    w = configs.dambreak_double()
+    p, pos, vel = _state(w, 20)
+    _compare(p, pos, vel, ref)
+
+
+def test_reference_step_time(ref):
+    """Steps per second of the reference's kernels (default nvcc flags) and
+    of the fused step on the 1M double dam break, from the same state."""
+    import torch
+    w = configs.dambreak_double()
+    p, pos, vel = _state(w, 200)
+    r = ref.RefStep(p, pos, vel, fast=True)
+    r.update(2)
+    stage = {}
+    k = 10
+    t0 = time.perf_counter()
+    r.update(k, stage)
+    ref_ms = (time.perf_counter() - t0) / k * 1e3
+    with SPH(p) as s:
+        s.set_array(ARRAY_POS, pos)
+        s.set_array(ARRAY_VEL, vel)
+        s.update(5)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.update(50)
+        torch.cuda.synchronize()
+        ours_ms = (time.perf_counter() - t0) / 50 * 1e3
+    line = {"workload": "double dam break, 1,048,576 particles, steps 200-212",
+            "reference_gpu_ms_per_step": ref_ms,
+            "reference_gpu_stage_ms": {kk: v / k * 1e3 for kk, v in stage.items()},
+            "fused_ms_per_step": ours_ms, "speedup": ref_ms / ours_ms}
+    print(json.dumps(line))
+    assert ours_ms < ref_ms
