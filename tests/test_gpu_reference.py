@@ -9,9 +9,10 @@ density with pow(c, 3) and contracts nothing (built with --fmad=false, like
 its host build that pins the oracle), the fused step with FMAs in the
 places the oracle has them.
 
-The last test times the reference's step (nvcc's default flags, every
+The last tests time the reference's step (nvcc's default flags, every
 wrapper synchronising as the reference's do) against the fused step on the
-1,048,576-particle double dam break and prints one JSON line.
+three single-scene workloads (32,768, 1,048,576 and 16,777,216 particles) and
+print one JSON line each.
 """
 import json
 import time
@@ -84,12 +85,30 @@ def test_double_dam_break_1m(ref):
     _compare(p, pos, vel, ref)
 
 
-def test_reference_step_time(ref):
-    """Steps per second of the reference's kernels (default nvcc flags) and
-    of the fused step on the 1M double dam break, from the same state."""
+def test_uniform_stress_16m(ref):
+    """16,777,216 particles uniform-random in the lower 60% of a 4x1x4 box
+    (2.96 M cells), after 3 steps."""
+    w = configs.uniform_stress()
+    p, pos, vel = _state(w, 3)
+    _compare(p, pos, vel, ref)
+
+
+TIMED = {
+    "single dam break, 32,768 particles": (lambda: configs.dambreak_small(side=32), 200),
+    "double dam break, 1,048,576 particles": (lambda: configs.dambreak_double(), 200),
+    "uniform stress, 16,777,216 particles": (lambda: configs.uniform_stress(), 3),
+}
+
+
+@pytest.mark.parametrize("name", list(TIMED))
+def test_reference_step_time(ref, name):
+    """Step time of the reference's kernels (default nvcc flags, each wrapper
+    synchronising) and of the fused step, from the same state after the
+    given number of fused steps."""
     import torch
-    w = configs.dambreak_double()
-    p, pos, vel = _state(w, 200)
+    make, warm = TIMED[name]
+    w = make()
+    p, pos, vel = _state(w, warm)
     r = ref.RefStep(p, pos, vel, fast=True)
     r.update(2)
     stage = {}
@@ -106,9 +125,12 @@ def test_reference_step_time(ref):
         s.update(50)
         torch.cuda.synchronize()
         ours_ms = (time.perf_counter() - t0) / 50 * 1e3
-    line = {"workload": "double dam break, 1,048,576 particles, steps 200-212",
+    n = len(pos)
+    line = {"workload": f"{name}, steps {warm}-{warm + 12} (reference), {warm}-{warm + 55} (fused)",
             "reference_gpu_ms_per_step": ref_ms,
+            "reference_gpu_particle_steps_per_s": n / ref_ms * 1e3,
             "reference_gpu_stage_ms": {kk: v / k * 1e3 for kk, v in stage.items()},
-            "fused_ms_per_step": ours_ms, "speedup": ref_ms / ours_ms}
+            "fused_ms_per_step": ours_ms, "fused_particle_steps_per_s": n / ours_ms * 1e3,
+            "speedup": ref_ms / ours_ms}
     print(json.dumps(line))
     assert ours_ms < ref_ms
