@@ -88,16 +88,21 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str):
-    """Per-launch DRAM bytes (read + write) of `kernel` from the committed ncu
-    summary of this workload (profiles/); None if it has no entry."""
+def ncu_summary(key: str, kernel: str):
+    """A per-launch figure of `kernel` from the committed ncu summary of this
+    workload (profiles/): `traffic` (DRAM bytes read + written) or `issue`
+    (fraction of issue slots busy); None if it has no entry."""
     path = os.path.join(ROOT, "profiles", "walk_kernels_double_dambreak_1M.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.startswith(f"traffic {kernel}:"):
+        if line.startswith(f"{key} {kernel}:"):
             return float(line.split(":")[1].split()[0])
     return None
+
+
+def ncu_traffic(kernel: str):
+    return ncu_summary("traffic", kernel)
 
 
 class ClockSampler:
@@ -540,10 +545,13 @@ def main():
     peak, peak_kind = measured_peaks()
     achieved = alg / (stage_ms[dom] / 1e3) / 1e9
     traffic = ncu_traffic(f"k_{dom}")
+    issue = ncu_summary("issue", f"k_{dom}")
     roofline = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                 "algorithmic_bytes": alg, "peak_source": peak_kind,
-                "stage_ms": stage_ms}
+                "stage_ms": stage_ms,
+                "binding": {"resource": "instruction issue", "issue_active_frac": issue,
+                            "source": "profiles/walk_kernels_double_dambreak_1M.md (ncu, crowded state)"}}
     P = 4 if p.numCells >= 65536 else 2
     model_b = 256 + 24 * P + 12 * p.numCells / n
     step_gbs = model_b * n / (total_ms / args.steps / 1e3) / 1e9
