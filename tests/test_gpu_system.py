@@ -294,6 +294,36 @@ def test_crowded_cells_keep_stable_order(cuda):
     np.testing.assert_array_equal(cs, o["cell_start"])
 
 
+def test_cell_sort_size_boundaries(cuda):
+    """One cell at each boundary of the cell sorts: the warp networks of 2,
+    4, 8, 16 and 32 ids per lane (33-64, ..., 513-1024 ids), the block sort
+    (1025-16384) and the sort through global scratch (above 16384), with the
+    ids of each cell scattered through the input; sorted pairs and cell
+    starts equal the oracle's."""
+    rng = np.random.default_rng(11)
+    h = configs.H_DAMBREAK
+    sizes = [33, 64, 65, 128, 129, 256, 257, 512, 513, 1024, 1025, 16384, 16385]
+    parts = []
+    for k, n in enumerate(sizes):
+        cx, cy = (2 + 2 * (k % 8)) * h, (2 + 2 * (k // 8)) * h
+        lo = np.array([cx, cy, 4 * h]) + 0.35 * h  # inside one cell, away from its faces
+        parts.append(rng.uniform(lo, lo + 0.3 * h, (n, 3)))
+    pos = np.ones((sum(sizes), 4), np.float32)
+    pos[:, :3] = np.concatenate(parts)
+    pos = pos[rng.permutation(len(pos))]
+    vel = np.zeros_like(pos)
+    xml = configs.scene_xml(**configs.dambreak_attrs(len(pos), (0, 0, 0), (1, 1, 1)))
+    p = Scene.parse(xml).params
+    with system_from(p, pos, vel) as s:
+        s.update(1)
+        sh, cs, _ = s.cells()
+    o = oracle.full_stages(p, pos, vel)
+    cnt = np.bincount(o["sorted"][:, 0], minlength=p.numCells)
+    assert sorted(cnt[cnt > 0].tolist()) == sorted(sizes)
+    np.testing.assert_array_equal(sh, o["sorted"])
+    np.testing.assert_array_equal(cs, o["cell_start"])
+
+
 @pytest.mark.parametrize("case", ["features", "foam"])
 def test_fused_color_and_dye(cuda, golden, case):
     """Colour and dye from the fused step against the reference's collide()
