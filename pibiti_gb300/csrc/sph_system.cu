@@ -514,6 +514,45 @@ __device__ __forceinline__ void force_item(const SceneDesc* __restrict__ sc,
   }
 }
 
+// Which thread of the block runs which of its particles does not change a
+// result, only how alike the lanes of a warp are: a lane's work in the
+// masked walk is its neighbours row by row (rows are (z, y) offsets), and the
+// warp waits for its busiest lane in every row.  Particles that sit at
+// nearby z, then y, within the same cell have similar row counts, so the
+// block hands its particles out in the order of the key (cell - the block's
+// first cell, z and y within the cell in sixteenths, thread), sorted in shared
+// memory.  At the crowded state this takes the lanes busy from ~59% to ~74%
+// (a model of the walk on that state's masks).
+template <int kThreads>
+__device__ __forceinline__ uint32_t regrouped_particle(const SceneDesc* __restrict__ sc,
+                                                       const uint32_t* __restrict__ poff, int S, uint32_t N,
+                                                       const float4* __restrict__ pos) {
+  static_assert(kThreads <= 256, "thread index in the key's low 8 bits");
+  __shared__ uint32_t skey[kThreads];
+  __shared__ uint32_t sbase;
+  const uint32_t t = threadIdx.x, i = blockIdx.x * kThreads + t;
+  uint32_t cell = 0, sub = 0;
+  if (i < N) {
+    const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
+    const SimParams& p = d.p;
+    const float4 x = pos[i];
+    const float gz = __fdiv_rn(__fsub_rn(x.z, p.worldMin.z), p.cellSize.z);
+    const float gy = __fdiv_rn(__fsub_rn(x.y, p.worldMin.y), p.cellSize.y);
+    cell = d.c_off + cell_of(p, grid_pos(p, x));
+    const uint32_t sz = (uint32_t)min(max((int)((gz - floorf(gz)) * 16.f), 0), 15);
+    const uint32_t sy = (uint32_t)min(max((int)((gy - floorf(gy)) * 16.f), 0), 15);
+    sub = (sz << 4) | sy;
+  }
+  if (t == 0) sbase = cell;  // the block's first particle (always < N)
+  __syncthreads();
+  const uint32_t d = cell - sbase;
+  skey[t] = i < N ? (min(d, 0x7FFFu) << 16) | (sub << 8) | t : 0xFFFFFFFFu;
+  __syncthreads();
+  bitonic(skey, kThreads, t, kThreads, [] { __syncthreads(); });
+  const uint32_t k = skey[t];
+  return k == 0xFFFFFFFFu ? 0xFFFFFFFFu : blockIdx.x * kThreads + (k & 0xFFu);
+}
+
 template <bool kMask, int kThreads, int kMinBlocks, bool kFeat>
 __global__ void __launch_bounds__(kThreads, kFeat ? kMinBlocks * 7 / 8 : kMinBlocks)
 k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
@@ -521,7 +560,8 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
         const float* __restrict__ dens, const float2* __restrict__ dp,
         const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
         const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out, FeatOut fo) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = kMask ? regrouped_particle<kThreads>(sc, poff, S, N, pos)
+                           : blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   force_item<kMask, kFeat>(sc, poff, S, N, pos, vel, dens, dp, start, count, masks, vel_out, fo, i);
 }
