@@ -632,9 +632,8 @@ __global__ void k_apply_correction(const SceneDesc* __restrict__ sc, const uint3
 // for a caller that asked for them, after the force pass: clr and dye are
 // in original order (the dye is read and written: it carries over between
 // steps).  The velocity increment is taken as v_new - v_start; the CLR_Vel
-// foam sum walks the in-grid neighbour cells in the reference's x-outer
-// order over the same truncated cell contents (the reference also visits
-// the wrapped cells beyond the grid edge, which the fused step skips).
+// foam sum walks the reference's 27 wrapped cell hashes in its x-outer
+// order over the same truncated cell contents.
 __global__ void k_color(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S,
                         uint32_t N, const float4* __restrict__ pos,
                         const float4* __restrict__ vel_start, const float4* __restrict__ vel_new,
@@ -649,19 +648,37 @@ __global__ void k_color(const SceneDesc* __restrict__ sc, const uint32_t* __rest
   const float3 add = make_float3(__fsub_rn(vn.x, vi.x), __fsub_rn(vn.y, vi.y), __fsub_rn(vn.z, vi.z));
   float vdiff = 0.f;
   if (p.clrType == SPH_CLR_VEL) {
+    // The reference's walk (System.cu:440-462) visits the 27 wrapped hashes
+    // of the unclamped cell (calcGridHash): a hash outside the table fetches
+    // cellStart 0 from the texture and stops at its first particle, whose
+    // hash cannot match; an in-table hash is a cell, possibly on the other
+    // side of the grid (its particles count while within the foam radius
+    // of 3).  Fetches past the scene's particles return zero, whose hash 0
+    // matches cell 0: an empty cell 0 yields one term with a zero
+    // neighbour, a cell 0 that ends the particle list one per missing slot.
     const int3 g = grid_pos(p, xi);
-    const int gx = (int)p.gridSize.x, gy = (int)p.gridSize.y, gz = (int)p.gridSize.z;
-    const int cx = min(max(g.x, 0), gx - 1), cy = min(max(g.y, 0), gy - 1), cz = min(max(g.z, 0), gz - 1);
+    const uint32_t ns = p.numParticles;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int x = -1; x < 2; ++x)
       for (int y = -1; y < 2; ++y)
         for (int z = -1; z < 2; ++z) {
-          const int ux = cx + x, uy = cy + y, uz = cz + z;
-          if (ux < 0 || ux >= gx || uy < 0 || uy >= gy || uz < 0 || uz >= gz) continue;
-          const uint32_t c = d.c_off + (uint32_t)(uz * (int)p.gridSize_yx + uy * gx + ux);
-          const uint32_t n = min(__ldg(count + c), p.maxParInCell), s0 = __ldg(start + c);
-          for (uint32_t q = 0; q < n; ++q) {
-            const uint32_t j = s0 + q;
-            if (j != i) vdiff = __fadd_rn(vdiff, foam_term(xi, vi, __ldg(pos + j), __ldg(vel_start + j)));
+          const uint32_t gh = grid_hash_raw(p, g.x + x, g.y + y, g.z + z);
+          if ((int)gh < 0 || gh >= p.numCells) continue;
+          const uint32_t c = d.c_off + gh, n = __ldg(count + c);
+          if (n == 0) {
+            if (gh == 0) vdiff = __fadd_rn(vdiff, foam_term(xi, vi, zero, zero));
+            continue;
+          }
+          const uint32_t s0 = __ldg(start + c), s0_local = s0 - d.p_off;
+          for (uint32_t q = 0; q < p.maxParInCell; ++q) {
+            if (q < n) {
+              const uint32_t j = s0 + q;
+              if (j != i) vdiff = __fadd_rn(vdiff, foam_term(xi, vi, __ldg(pos + j), __ldg(vel_start + j)));
+            } else if (s0_local + q >= ns && gh == 0) {
+              vdiff = __fadd_rn(vdiff, foam_term(xi, vi, zero, zero));
+            } else {
+              break;  // the next particle belongs to another cell
+            }
           }
         }
   }

@@ -156,6 +156,42 @@ def make_steps():
     pf.clrType = 3
     save_step("foam", pf, posc, velc, "CLR_Vel foam colour with dye")
 
+    # C3: the CLR_Vel colour at the grid's edges: cell 0 empty with particles
+    #     around it (its walk fetches a zero hash that matches cell 0), and
+    #     particles in the last x column, whose +x neighbours wrap to the
+    #     first cells of the next row (calcGridHash), which are occupied.
+    #     Soft walls off, so that one step keeps the particles in their cells
+    #     (the hard clamp is half a cell from the wall).
+    rng = np.random.default_rng(13)
+    pf = pf.copy()
+    pf.distBndSoft = 0.0
+    cs_ = np.array([pf.cellSize.x, pf.cellSize.y, pf.cellSize.z])
+    gx = int(pf.gridSize.x)
+
+    def in_cells(cells, k):
+        cells = np.asarray(cells, float)
+        c = cells[rng.integers(0, len(cells), k)]
+        lo = np.where(c == 0, 0.6, np.where(c == gx - 1, 0.05, 0.3))
+        hi = np.where(c == 0, 0.9, np.where(c == gx - 1, 0.35, 0.7))
+        return wmin + (c + rng.uniform(lo, hi)) * cs_
+
+    low = [(x, y, z) for x in (0, 1) for y in (0, 1) for z in (0, 1) if (x, y, z) != (0, 0, 0)]
+    edge = [(gx - 1, 0, z) for z in (0, 1)]
+    pe = np.ones((1024, 4), np.float32)
+    pe[:, :3] = np.concatenate([in_cells(low, 768), in_cells(edge, 256)])
+    ve = np.zeros((1024, 4), np.float32)
+    ve[:, :3] = rng.normal(0, 0.3, (1024, 3))
+    save_step("foam_edges", pf, pe, ve, "CLR_Vel foam: empty cell 0, wrapped neighbour cells")
+
+    # C4: ten particles, all in cell 0 (fewer than maxParInCell): the walk of
+    #     cell 0 runs past the last particle, where fetches return hash 0
+    pt = np.ones((10, 4), np.float32)
+    pt[:, :3] = wmin + rng.uniform(0.6, 0.7, (10, 3)) * cs_
+    vt = np.zeros((10, 4), np.float32)
+    vt[:, :3] = rng.normal(0, 0.02, (10, 3))
+    assert pf.maxParInCell > 10
+    save_step("foam_tiny", pf, pt, vt, "CLR_Vel foam: all particles in cell 0")
+
     # D: a grid of more than 65536 cells: 32-bit sort passes
     wd = configs.dambreak_small(side=8)
     xmld = configs.scene_xml(**configs.dambreak_attrs(1024, (0.0, 0.0, 0.0), (2.2, 2.0, 2.2)))

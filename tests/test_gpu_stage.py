@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 DENS_RTOL = 1e-5
 VEL_RTOL = 1e-5
-CASES = ["dambreak", "truncate", "features", "foam", "bigrid", "tiny", "rotor", "propeller",
+CASES = ["dambreak", "truncate", "features", "foam", "foam_edges", "foam_tiny", "bigrid", "tiny", "rotor", "propeller",
          "hmapxz", "hmapyz"]
 
 

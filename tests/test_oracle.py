@@ -138,7 +138,7 @@ def test_live_reference(case, golden):
     np.testing.assert_allclose(o["vel"], r["vel"], rtol=0, atol=VEL_RTOL * np.abs(r["vel"]).max())
 
 
-@pytest.mark.parametrize("case", ["features", "foam"])
+@pytest.mark.parametrize("case", ["features", "foam", "foam_edges", "foam_tiny"])
 def test_color_and_dye(golden, case):
     g = golden(f"step_{case}.npz")
     p = params_from(g["params"])
