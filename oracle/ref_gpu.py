@@ -95,6 +95,23 @@ def _load(fast: bool) -> ctypes.CDLL:
     return L
 
 
+def integrate(params, pos, vel, fast: bool = False):
+    """The reference's integrate wrapper (System.cu:653-667, with
+    boundary()) alone on the GPU: (new positions, new velocities)."""
+    import torch
+    L = _load(fast)
+    raw = params.to_bytes()
+    buf = ctypes.create_string_buffer(raw, len(raw))
+    _check(L.ref_gpu_set_params(buf, len(raw)), "setParameters")
+    n = len(pos)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32).reshape(n, 4)).cuda()  # noqa: E731
+    p0, v0 = dev(pos), dev(vel)
+    p1, v1 = torch.empty_like(p0), torch.empty_like(v0)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    _check(L.ref_gpu_integrate(vp(p0), vp(p1), vp(v0), vp(v1), n), "integrate")
+    return p1.cpu().numpy(), v1.cpu().numpy()
+
+
 class RefStep:
     """The reference's buffers (cSPH, SPH_Mem.cpp) for one scene of N
     particles on the GPU, and its Update.  N must be <= 64 or a multiple of
