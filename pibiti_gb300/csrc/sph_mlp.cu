@@ -452,23 +452,23 @@ int sm_count() {
 // ---- tcgen05 inference ------------------------------------------------------
 // The forward pass on the 5th-generation tensor cores: one CTA of 128
 // threads per 128-particle tile (grid-stride over tiles).  Each layer is a
-// tcgen05.mma (layer 1: 128x16 . 16x64, one instruction; layer 2: 128x64 .
-// 64x64 and layer 3: 128x64 . 64x16, four of K = 16 each) with BF16 operands
-// in shared memory (K-major core-matrix layout, no swizzle) and FP32
+// tcgen05.mma chain (layer 1: 128x16 . 16x64, one instruction; layer 2:
+// 128x64 . 64x64 and layer 3: 128x64 . 64x16, four of K = 16 each) with BF16
+// operands in shared memory (K-major core-matrix layout, no swizzle) and FP32
 // accumulators in one 64-column TMEM allocation that the three layers use in
-// turn.  Each warp reads its 32 rows (TMEM lanes 32w..32w+31) back with
-// tcgen05.ld; each layer's accumulators start from its bias (tcgen05.st),
-// tanh runs in registers and the BF16 activations go back to shared memory
-// as the next layer's A operand.  The input tile, the
-// layer-1 and the layer-2 activations share one buffer: each is dead once
-// the MMA that reads it has completed.  Only outputs 0..2 of layer 3 are
-// kept, so rows 3..15 of its B operand are don't-care: row 3 holds b3,
-// rows 4..7 the biases b1 and b2, rows 8..15 are the first bytes of W2^T.  That keeps a
-// CTA at 27.0 KB of shared memory, so 8 fit an SM with 8 x 64 = 512 TMEM
-// columns.  Thread 0 issues the MMAs and commits
-// them to one mbarrier; every wait on it is bounded (kTcSpins polls), after
-// which the CTA records an error (sph_mlp_status), writes NaN to the rows it
-// did not finish, and still frees its TMEM.
+// turn.  Each layer's accumulators start from its bias (tcgen05.st), as the
+// mma.sync pass's fragments do, so both round the same sums.  Each warp reads
+// its 32 rows (TMEM lanes 32w..32w+31) back with tcgen05.ld; tanh runs in
+// registers and the BF16 activations go back to shared memory as the next
+// layer's A operand.  The input tile and the layer-1 and layer-2 activations
+// share one buffer: each is dead once the MMA that reads it has completed.
+// Only outputs 0..2 of layer 3 are kept, so rows 3..15 of its B operand are
+// don't-care: row 3 holds b3, rows 4..7 the biases b1 and b2, rows 8..15 are
+// the first bytes of W2^T.  That keeps a CTA at 27.0 KB of shared memory, so
+// 8 fit an SM with 8 x 64 = 512 TMEM columns.  Thread 0 issues the MMAs and
+// commits them to one mbarrier; every wait on it is bounded (kTcSpins polls),
+// after which the CTA records an error (sph_mlp_status), writes NaN to the
+// rows it did not finish, and still frees its TMEM.
 namespace tcg {
 constexpr uint32_t kTcSpins = 1u << 22;
 // shared memory (bytes)
