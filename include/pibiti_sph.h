@@ -254,6 +254,11 @@ int sph_mlp_forward(const void* packed, const uint16_t* x, uint32_t n, float* y,
    uses this pass; its density check treats NaN as a failed coarse step. */
 int sph_mlp_forward_tc(const void* packed, const uint16_t* x, uint32_t n, float* y, void* stream);
 int sph_mlp_status(uint32_t* status);
+/* Test hook for the timeout path of sph_mlp_forward_tc: the same launch
+   with the tensor-core work withheld and each wait bounded at 1024 polls,
+   so every thread block's first wait runs out: all n rows become NaN, status
+   bit 0 is set, and the tensor memory is freed (a later pass runs normally). */
+int sph_mlp_forward_tc_withheld(const void* packed, const uint16_t* x, uint32_t n, float* y, void* stream);
 /* One pass over n samples of the loss mean((y - target)^2) (over all 3n
    outputs): adds d loss / d params to grad[5443] and the loss to *loss
    (both FP32, zeroed by the caller). */

@@ -112,6 +112,7 @@ SIGNATURES = {
     "sph_mlp_pack": [vp, vp, vp],
     "sph_mlp_forward": [vp, vp, u32, vp, vp],
     "sph_mlp_forward_tc": [vp, vp, u32, vp, vp],
+    "sph_mlp_forward_tc_withheld": [vp, vp, u32, vp, vp],
     "sph_mlp_status": [P(u32)],
     "sph_mlp_train_pass": [vp, vp, vp, u32, vp, vp, vp],
     "sph_mlp_adam": [vp, vp, vp, vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,

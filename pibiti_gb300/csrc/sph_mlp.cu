@@ -524,8 +524,8 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t phase) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
-  for (uint32_t k = 0; k < kTcSpins; ++k)
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, uint32_t spins) {
+  for (uint32_t k = 0; k < spins; ++k)
     if (mbar_try(bar, phase)) return true;
   return false;
 }
@@ -625,9 +625,12 @@ __device__ __forceinline__ void activate(uint32_t lane_base, uint8_t* hbuf, uint
 
 __device__ uint32_t g_tc_status;  // non-zero: a tcgen05 wait ran out (sph_mlp_status)
 
+// `spins` bounds each wait; `withhold` (a test of the timeout path) issues
+// no MMA and commits nothing, so that the first wait runs out.
 __global__ void __launch_bounds__(128, tcg::kBlocksPerSm) k_forward_tc(const uint16_t* __restrict__ img,
                                                                        const uint16_t* __restrict__ x,
-                                                                       uint32_t n, float* __restrict__ y) {
+                                                                       uint32_t n, float* __restrict__ y,
+                                                                       uint32_t spins, bool withhold) {
   using namespace tcg;
   extern __shared__ __align__(128) uint8_t sm[];
   const uint32_t t = threadIdx.x, w = t >> 5;
@@ -679,12 +682,12 @@ __global__ void __launch_bounds__(128, tcg::kBlocksPerSm) k_forward_tc(const uin
   bool ok = true, pending = false;
   // thread 0 issues, everyone waits (bounded); false when the wait ran out
   auto run = [&](auto issue) {
-    if (t == 0) {
+    if (t == 0 && !withhold) {
       issue();
       commit(sb + oBar);
     }
-    pending = true;
-    ok = __syncthreads_and(mbar_wait(sb + oBar, phase));
+    pending = !withhold;
+    ok = __syncthreads_and(mbar_wait(sb + oBar, phase, spins));
     if (!ok) return false;
     pending = false;
     phase ^= 1u;
@@ -733,7 +736,7 @@ __global__ void __launch_bounds__(128, tcg::kBlocksPerSm) k_forward_tc(const uin
   }
   if (!ok) {
     if (t == 0) atomicOr(&g_tc_status, 1u);
-    if (pending) __syncthreads_and(mbar_wait(sb + oBar, phase));  // the MMAs still in flight
+    if (pending) __syncthreads_and(mbar_wait(sb + oBar, phase, spins));  // the MMAs still in flight
     // the rows this CTA did not finish become NaN, which a caller's
     // finiteness check sees
     for (; tile < tiles; tile += gridDim.x) {
@@ -775,8 +778,20 @@ int sph_mlp_forward_tc(const void* packed, const uint16_t* x, uint32_t n, float*
   if (n == 0) return SPH_OK;
   const uint32_t tiles = (n + 127) / 128;
   const uint32_t blocks = (uint32_t)min((long long)tiles, (long long)sm_count() * tcg::kBlocksPerSm);
-  k_forward_tc<<<blocks, 128, tcg::kSmem, (cudaStream_t)stream>>>((const uint16_t*)packed, x, n, y);
+  k_forward_tc<<<blocks, 128, tcg::kSmem, (cudaStream_t)stream>>>((const uint16_t*)packed, x, n, y,
+                                                                  tcg::kTcSpins, false);
   return cuda_check(cudaGetLastError(), "mlp_forward_tc");
+}
+
+int sph_mlp_forward_tc_withheld(const void* packed, const uint16_t* x, uint32_t n, float* y, void* stream) {
+  if (!packed || (!x && n) || (!y && n)) return fail(SPH_ERR_ARG, "mlp_forward_tc_withheld: null pointer");
+  if ((uintptr_t)x & 15u) return fail(SPH_ERR_ARG, "mlp_forward_tc_withheld: features not 16-byte aligned");
+  if (n == 0) return SPH_OK;
+  const uint32_t tiles = (n + 127) / 128;
+  const uint32_t blocks = (uint32_t)min((long long)tiles, (long long)sm_count() * tcg::kBlocksPerSm);
+  k_forward_tc<<<blocks, 128, tcg::kSmem, (cudaStream_t)stream>>>((const uint16_t*)packed, x, n, y, 1024u,
+                                                                  true);
+  return cuda_check(cudaGetLastError(), "mlp_forward_tc_withheld");
 }
 
 int sph_mlp_status(uint32_t* status) {

@@ -90,6 +90,33 @@ def test_forward_tc(cuda, n):
     np.testing.assert_array_equal(a, b)
 
 
+def test_forward_tc_timeout_path(cuda):
+    """A pass whose tensor-core work is withheld (test hook): every thread
+    block's wait runs out; its rows become NaN, the status word reports it
+    once, and the next pass runs normally (the tensor memory was freed)."""
+    torch = cuda
+    _l, L = _lib()
+    n = 100_003
+    rng = np.random.default_rng(3)
+    _, img = _pack(torch, omlp.init(2))
+    xd = _x(torch, rng.normal(0, 1, size=(n, 16)).astype(np.float32))
+    y = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
+    _l.check(L.sph_mlp_forward_tc_withheld(_p(img), _p(xd), n, _p(y), None))
+    status = ctypes.c_uint32(0)
+    _l.check(L.sph_mlp_status(ctypes.byref(status)))
+    assert status.value == 1
+    assert bool(torch.isnan(y).all())
+    _l.check(L.sph_mlp_status(ctypes.byref(status)))
+    assert status.value == 0
+    y_tc = torch.zeros_like(y)
+    y_mma = torch.zeros_like(y)
+    _l.check(L.sph_mlp_forward_tc(_p(img), _p(xd), n, _p(y_tc), None))
+    _l.check(L.sph_mlp_forward(_p(img), _p(xd), n, _p(y_mma), None))
+    _l.check(L.sph_mlp_status(ctypes.byref(status)))
+    assert status.value == 0
+    assert torch.equal(y_tc, y_mma)
+
+
 def test_forward_tc_arguments(cuda):
     torch = cuda
     _l, L = _lib()
