@@ -181,10 +181,16 @@ int sph_set_color_output(SphSystem* sys, sph_float4* clr, float* dye);
    one cooperative launch (all blocks resident, a grid barrier between the
    stages, the same per-particle code as the launch-per-stage path, so the
    same results bit for bit).  A barrier wait that does not end within its
-   poll limit sets bit 4 of sph_flags and the kernel returns early.  Needs
-   the neighbour masks (maxParInCell <= 21) and a device with cooperative
-   launch; not used while a colour output is set. */
+   poll limit sets bit 2 (value 4) of sph_flags and the kernel returns
+   early.  Needs the neighbour masks (maxParInCell <= 21) and a device with
+   cooperative launch; not used while a colour output is set. */
 int sph_set_persistent(SphSystem* sys, int on);
+/* Test hook for that timeout: one persistent step in which block 0 leaves
+   before the first barrier and each wait is bounded at 4096 polls, so the
+   other blocks' waits run out and the kernel ends; *flags gets sph_flags
+   (bit 2 set).  Only scratch arrays are written: the state does not advance
+   and the handle stays usable.  Needs persistent stepping on. */
+int sph_persistent_withheld(SphSystem* sys, uint32_t* flags);
 
 /* Launch shape of the density and force walks: 0 = 64 threads per block,
    1 = 128 (default), 2 = 256, each compiled for full occupancy at that size. */

@@ -85,6 +85,7 @@ SIGNATURES = {
     "sph_set_graph_steps": [vp, u32],
     "sph_set_color_output": [vp, vp, vp],
     "sph_set_persistent": [vp, i32],
+    "sph_persistent_withheld": [vp, P(u32)],
     "sph_set_walk_shape": [vp, u32],
     "sph_get_walk_shape": [vp, P(u32), P(u32)],
     "sph_autotune": [vp, u32, P(ctypes.c_float), P(u32)],

@@ -825,8 +825,8 @@ __global__ void __launch_bounds__(kBlock) k_stats(const SceneDesc* __restrict__ 
 // kernels use, with a grid barrier between stages, so the results are those
 // of enqueue_step bit for bit.  The launch is cooperative, so all blocks are
 // resident; the barrier's waits are bounded: after kBarrierSpins polls a
-// block sets bit 4 of `flags` and the barrier status, and every block leaves
-// at its next barrier.
+// block sets bit 2 (kFlagBarrier) of `flags` and the barrier status, and
+// every block leaves at its next barrier.
 constexpr int kPThreads = 256;
 constexpr int kPWarps = kPThreads / 32;
 constexpr uint32_t kPTile = kPThreads * 8;            // scan tile
@@ -850,6 +850,8 @@ struct PersistArgs {
   uint32_t* bar;  // [arrived, generation, status]
   uint32_t steps;
   int cp, cv;
+  uint32_t spins;   // poll limit of a barrier wait (kBarrierSpins)
+  uint32_t absent;  // a block that leaves at once (a test of the timeout), or ~0u
 };
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
@@ -860,7 +862,7 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
 
 // Sense-reversing grid barrier: the last block to arrive resets the count
 // and advances the generation; the others poll the generation (acquire).
-__device__ bool grid_barrier(uint32_t* bar, uint32_t* flags) {
+__device__ bool grid_barrier(uint32_t* bar, uint32_t* flags, uint32_t max_spins) {
   __syncthreads();
   if (threadIdx.x == 0) {
     const uint32_t g = ld_acquire(bar + 1);
@@ -872,7 +874,7 @@ __device__ bool grid_barrier(uint32_t* bar, uint32_t* flags) {
     } else {
       uint32_t spins = 0;
       while (ld_acquire(bar + 1) == g) {
-        if (++spins > kBarrierSpins) {
+        if (++spins > max_spins) {
           atomicOr(bar + 2, 1u);
           atomicOr(flags, kFlagBarrier);
           break;
@@ -921,17 +923,18 @@ __global__ void __launch_bounds__(kPThreads, 4) k_persistent(PersistArgs a) {
   float4* vel_v = a.cv ? a.vel1 : a.vel0;
   float4* vel_o = a.cv ? a.vel0 : a.vel1;
   int cp = a.cp;
+  if (blockIdx.x == a.absent) return;
   for (uint32_t step = 0; step < a.steps; ++step) {
     float4 *pa = cp ? a.pos1 : a.pos0, *pb = cp ? a.pos0 : a.pos1;
     uint32_t *ia = cp ? a.id1 : a.id0, *ib = cp ? a.id0 : a.id1;
     // clear the cell counts and the sort lists
     for (uint32_t c = tid; c < a.C; c += nthr) a.count[c] = 0u;
     if (tid == 0) a.sort_counters[0] = a.sort_counters[1] = 0u;
-    if (!grid_barrier(a.bar, a.flags)) return;
+    if (!grid_barrier(a.bar, a.flags, a.spins)) return;
     // integrate and count (whole warps over consecutive particles)
     for (uint32_t base = gwarp * 32; base < a.N; base += nwarps * 32)
       integrate_count_item(a.sc, a.poff, a.S, a.N, pa, vel_v, a.key, a.rank, a.count, a.flags, base + lane);
-    if (!grid_barrier(a.bar, a.flags)) return;
+    if (!grid_barrier(a.bar, a.flags, a.spins)) return;
     // exclusive scan count -> start: tile sums, their scan (block 0), tiles
     for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
       uint32_t sum = 0, tot;
@@ -942,7 +945,7 @@ __global__ void __launch_bounds__(kPThreads, 4) k_persistent(PersistArgs a) {
       p_block_scan(sum, wtot, &tot);
       if (threadIdx.x == 0) a.tsum[t] = tot;
     }
-    if (!grid_barrier(a.bar, a.flags)) return;
+    if (!grid_barrier(a.bar, a.flags, a.spins)) return;
     if (blockIdx.x == 0) {
       uint32_t carry = 0;
       for (uint32_t t0 = 0; t0 < tiles; t0 += kPThreads) {
@@ -954,7 +957,7 @@ __global__ void __launch_bounds__(kPThreads, 4) k_persistent(PersistArgs a) {
         carry += tot;
       }
     }
-    if (!grid_barrier(a.bar, a.flags)) return;
+    if (!grid_barrier(a.bar, a.flags, a.spins)) return;
     for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x) {
       uint32_t v[8], sum = 0, tot;
       for (uint32_t k = 0; k < 8; ++k) {
@@ -969,7 +972,7 @@ __global__ void __launch_bounds__(kPThreads, 4) k_persistent(PersistArgs a) {
         run += v[k];
       }
     }
-    if (!grid_barrier(a.bar, a.flags)) return;
+    if (!grid_barrier(a.bar, a.flags, a.spins)) return;
     // ids into their cells; cells that need their ids sorted
     for (uint32_t i = tid; i < a.N; i += nthr) a.slot[a.start[a.key[i]] + a.rank[i]] = ia[i];
     for (uint32_t base = gwarp * 32; base < a.C; base += nwarps * 32) {
@@ -988,7 +991,7 @@ __global__ void __launch_bounds__(kPThreads, 4) k_persistent(PersistArgs a) {
       if (mid) a.sort_list[base_m + (uint32_t)__popc(bm & below)] = c;
       if (big) a.big_list[base_b + (uint32_t)__popc(bb & below)] = c;
     }
-    if (!grid_barrier(a.bar, a.flags)) return;
+    if (!grid_barrier(a.bar, a.flags, a.spins)) return;
     // sort: a warp per listed cell, then a block per big cell
     {
       const uint32_t nl = *((volatile uint32_t*)a.sort_counters);
@@ -1015,20 +1018,20 @@ __global__ void __launch_bounds__(kPThreads, 4) k_persistent(PersistArgs a) {
         __syncthreads();
       }
     }
-    if (!grid_barrier(a.bar, a.flags)) return;
+    if (!grid_barrier(a.bar, a.flags, a.spins)) return;
     for (uint32_t i = tid; i < a.N; i += nthr)
       place_item(a.sc, a.poff, a.S, a.N, pa, vel_v, ia, a.key, a.start, a.count, a.slot, a.dest, pb, vel_o,
                  ib, nullptr, i);
-    if (!grid_barrier(a.bar, a.flags)) return;
+    if (!grid_barrier(a.bar, a.flags, a.spins)) return;
     for (uint32_t i = tid; i < a.N; i += nthr)
       density_item<true, false>(a.sc, a.poff, a.S, a.N, pb, a.start, a.count, a.dens, a.pres, a.dp, a.masks,
                          a.flags, i);
-    if (!grid_barrier(a.bar, a.flags)) return;
+    if (!grid_barrier(a.bar, a.flags, a.spins)) return;
     const FeatOut no_feat = {nullptr, nullptr, nullptr};
     for (uint32_t i = tid; i < a.N; i += nthr)
       force_item<true, false, false>(a.sc, a.poff, a.S, a.N, pb, vel_o, a.dens, a.dp, a.start, a.count,
                               a.masks, vel_v, no_feat, i);
-    if (!grid_barrier(a.bar, a.flags)) return;
+    if (!grid_barrier(a.bar, a.flags, a.spins)) return;
     cp = 1 - cp;
   }
 }
@@ -1467,8 +1470,11 @@ int sph_get_array(SphSystem* s, uint32_t which, sph_float4* out, int dst_on_devi
   return SPH_OK;
 }
 
-static int persistent_steps(SphSystem* s, uint32_t steps) {
+static int persistent_steps(SphSystem* s, uint32_t steps, uint32_t spins = kBarrierSpins,
+                            uint32_t absent = ~0u) {
   PersistArgs a;
+  a.spins = spins;
+  a.absent = absent;
   a.sc = s->d_scenes;
   a.poff = s->d_poff;
   a.S = s->S;
@@ -1507,6 +1513,15 @@ static int persistent_steps(SphSystem* s, uint32_t steps) {
            "persistent step launch");
   if (steps & 1) s->cp = 1 - s->cp;
   return SPH_OK;
+}
+
+int sph_persistent_withheld(SphSystem* s, uint32_t* flags) {
+  if (!s || !flags) return fail(SPH_ERR_ARG, "persistent_withheld: bad arguments");
+  if (!s->persistent || !s->persist_grid) return fail(SPH_ERR_ARG, "persistent_withheld: persistent stepping is off");
+  const int cp = s->cp;
+  SPH_TRY(persistent_steps(s, 1, 4096u, 0u));
+  s->cp = cp;  // the step did not happen
+  return sph_flags(s, flags);
 }
 
 int sph_set_persistent(SphSystem* s, int on) {

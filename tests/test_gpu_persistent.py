@@ -1,7 +1,8 @@
 """The persistent step (sph_set_persistent: k steps as one cooperative
 launch) against the launch-per-stage path: the same bits for one scene, for
 an ensemble of uneven scenes, and for crowded cells of every sort tier;
-no barrier timeout (bit 4 of the flags)."""
+no barrier timeout (bit 2 of the flags); and a forced timeout that leaves
+the handle usable."""
 import numpy as np
 import pytest
 
@@ -28,6 +29,29 @@ def _same(a, b):
     np.testing.assert_array_equal(a[1], b[1])
     np.testing.assert_array_equal(a[2], b[2])
     assert not (b[3] & 4), "persistent barrier timed out"
+
+
+def test_barrier_timeout_leaves_handle_usable(cuda):
+    """Block 0 withheld from the barriers (test hook): the other blocks'
+    bounded waits run out, flag bit 2 is set, the state does not advance,
+    and the handle then steps exactly as the launch-per-stage path does."""
+    import ctypes
+    from pibiti_gb300 import _lib
+    w = configs.dambreak_small(side=16)
+    p = Scene.parse(w.xml).params
+    expect = _run(p, w.pos, w.vel, [10], False)
+    with SPH(p) as s:
+        s.set_array(ARRAY_POS, w.pos)
+        s.set_array(ARRAY_VEL, w.vel)
+        s.set_persistent(True)
+        flags = ctypes.c_uint32(0)
+        _lib.check(_lib.lib().sph_persistent_withheld(s._h, ctypes.byref(flags)))
+        assert flags.value & 4
+        np.testing.assert_array_equal(s.get_array(ARRAY_POS), np.asarray(w.pos, np.float32))
+        np.testing.assert_array_equal(s.get_array(ARRAY_VEL), np.asarray(w.vel, np.float32))
+        s.update(10)
+        got = s.get_array(ARRAY_POS), s.get_array(ARRAY_VEL), s.cells()[0], s.flags()
+    _same(expect, got)
 
 
 @pytest.mark.parametrize("steps", [[40], [7, 1, 12]])
