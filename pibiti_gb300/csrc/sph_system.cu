@@ -45,6 +45,7 @@ namespace {
 struct __align__(16) SceneDesc {
   SimParams p;
   uint32_t p_off, p_cnt, c_off, c_cnt;
+  float inv_cell[3];  // 1 / cellSize (rounded; for scheduling keys only)
 };
 
 constexpr int kBlock = 256;
@@ -518,39 +519,49 @@ __device__ __forceinline__ void force_item(const SceneDesc* __restrict__ sc,
 // result, only how alike the lanes of a warp are: a lane's work in the
 // masked walk is its neighbours row by row (rows are (z, y) offsets), and the
 // warp waits for its busiest lane in every row.  Particles that sit at
-// nearby z, then y, within the same cell have similar row counts, so the
-// block hands its particles out in the order of the key (cell - the block's
-// first cell, z and y within the cell in sixteenths, thread), sorted in shared
-// memory.  At the crowded state this takes the lanes busy from ~59% to ~74%
-// (a model of the walk on that state's masks).
+// nearby z, then y, within the same cell have similar row counts, so a block
+// whose particles lie in a few crowded cells hands them out in the order of
+// the key (cell - the block's first cell, z and y within the cell in
+// sixteenths, thread), sorted in shared memory.  At the crowded state this
+// takes the lanes busy from ~59% to ~74% (a model of the walk on that state's
+// masks).  A block over more than kRegroupSpan cells (small cells: little to
+// gain) keeps its order and skips the sort.  The keys use the rounded
+// reciprocal of the cell size: a key off by one cell only regroups worse.
+constexpr uint32_t kRegroupSpan = 4;
+
 template <int kThreads>
 __device__ __forceinline__ uint32_t regrouped_particle(const SceneDesc* __restrict__ sc,
                                                        const uint32_t* __restrict__ poff, int S, uint32_t N,
                                                        const float4* __restrict__ pos) {
   static_assert(kThreads <= 256, "thread index in the key's low 8 bits");
   __shared__ uint32_t skey[kThreads];
-  __shared__ uint32_t sbase;
-  const uint32_t t = threadIdx.x, i = blockIdx.x * kThreads + t;
+  __shared__ uint32_t sfirst, slast;
+  const uint32_t t = threadIdx.x, i0 = blockIdx.x * kThreads, i = i0 + t;
   uint32_t cell = 0, sub = 0;
   if (i < N) {
     const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
     const SimParams& p = d.p;
-    const float4 x = pos[i];
-    const float gz = __fdiv_rn(__fsub_rn(x.z, p.worldMin.z), p.cellSize.z);
-    const float gy = __fdiv_rn(__fsub_rn(x.y, p.worldMin.y), p.cellSize.y);
-    cell = d.c_off + cell_of(p, grid_pos(p, x));
-    const uint32_t sz = (uint32_t)min(max((int)((gz - floorf(gz)) * 16.f), 0), 15);
-    const uint32_t sy = (uint32_t)min(max((int)((gy - floorf(gy)) * 16.f), 0), 15);
+    const float4 x = __ldg(pos + i);
+    const float gx = (x.x - p.worldMin.x) * d.inv_cell[0];
+    const float gy = (x.y - p.worldMin.y) * d.inv_cell[1];
+    const float gz = (x.z - p.worldMin.z) * d.inv_cell[2];
+    const float fx = floorf(gx), fy = floorf(gy), fz = floorf(gz);
+    cell = d.c_off + cell_of(p, make_int3((int)fx, (int)fy, (int)fz));
+    const uint32_t sz = (uint32_t)min(max((int)((gz - fz) * 16.f), 0), 15);
+    const uint32_t sy = (uint32_t)min(max((int)((gy - fy) * 16.f), 0), 15);
     sub = (sz << 4) | sy;
   }
-  if (t == 0) sbase = cell;  // the block's first particle (always < N)
+  const uint32_t last = min(N - 1 - i0, (uint32_t)kThreads - 1);
+  if (t == 0) sfirst = cell;  // the block's first particle (always < N)
+  if (t == last) slast = cell;
   __syncthreads();
-  const uint32_t d = cell - sbase;
-  skey[t] = i < N ? (min(d, 0x7FFFu) << 16) | (sub << 8) | t : 0xFFFFFFFFu;
+  const uint32_t base = sfirst;
+  if (slast - base > kRegroupSpan) return i;  // uniform over the block
+  skey[t] = i < N ? (min(cell - base, 0x7FFFu) << 16) | (sub << 8) | t : 0xFFFFFFFFu;
   __syncthreads();
   bitonic(skey, kThreads, t, kThreads, [] { __syncthreads(); });
   const uint32_t k = skey[t];
-  return k == 0xFFFFFFFFu ? 0xFFFFFFFFu : blockIdx.x * kThreads + (k & 0xFFu);
+  return k == 0xFFFFFFFFu ? 0xFFFFFFFFu : i0 + (k & 0xFFu);
 }
 
 template <bool kMask, int kThreads, int kMinBlocks, bool kFeat>
@@ -1111,6 +1122,9 @@ int upload_scenes(SphSystem* s) {
     h[i].p_cnt = s->poff[i + 1] - s->poff[i];
     h[i].c_off = s->coff[i];
     h[i].c_cnt = s->coff[i + 1] - s->coff[i];
+    h[i].inv_cell[0] = 1.f / h[i].p.cellSize.x;
+    h[i].inv_cell[1] = 1.f / h[i].p.cellSize.y;
+    h[i].inv_cell[2] = 1.f / h[i].p.cellSize.z;
   }
   SPH_CUDA(cudaMemcpyAsync(s->d_scenes, h.data(), sizeof(SceneDesc) * s->S, cudaMemcpyHostToDevice,
                            s->stream),
@@ -1674,6 +1688,9 @@ int ensure_coarse(SphSystem* s, uint32_t sub) {
     h[i].p_cnt = s->poff[i + 1] - s->poff[i];
     h[i].c_off = s->coff[i];
     h[i].c_cnt = s->coff[i + 1] - s->coff[i];
+    h[i].inv_cell[0] = 1.f / h[i].p.cellSize.x;
+    h[i].inv_cell[1] = 1.f / h[i].p.cellSize.y;
+    h[i].inv_cell[2] = 1.f / h[i].p.cellSize.z;
   }
   SPH_CUDA(cudaMemcpyAsync(s->d_coarse, h.data(), sizeof(SceneDesc) * s->S, cudaMemcpyHostToDevice,
                            s->stream),
