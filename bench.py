@@ -374,13 +374,18 @@ def measure_learned(w, p, stream, fine_steps: int = 2000, substeps: int = 4, tol
 
 def measure_render(sysm, p, stream, width: int = 1920, height: int = 1080, iterations: int = 8,
                    frames: int = 10):
-    """The headless renderer on the state the timed steps left: curvature
-    flow with `iterations` passes at width x height, wall time per frame
-    (each frame is synchronous; CUDA events bracket the frames)."""
+    """The headless renderer on the state the timed steps left (advanced by
+    one step with the colour output on, for the foam overlay's input):
+    curvature flow with `iterations` passes at width x height, wall time per
+    frame (each frame is synchronous), then the foam overlay alone."""
     import torch
     from pibiti_gb300.render import Renderer, look_at, perspective
     from pibiti_gb300.sph import ARRAY_POS
     pos = torch.empty((sysm.n, 4), dtype=torch.float32, device="cuda")
+    clr = torch.empty((sysm.n, 4), dtype=torch.float32, device="cuda")
+    sysm.set_color_output(clr)
+    sysm.update(1)
+    sysm.set_color_output(None)
     sysm.get_array(ARRAY_POS, out=pos)
     torch.cuda.synchronize()
     mv = look_at((3.0, 2.6, 6.8), (3.0, 0.6, 0.85))
@@ -394,11 +399,21 @@ def measure_render(sysm, p, stream, width: int = 1920, height: int = 1080, itera
             r.frame_params(pos, prm)
         ms = 1e3 * (time.perf_counter() - t0) / frames
         frags = r.fragments
+        rgba = r.frame_params(pos, prm)[2]
+        r.foam_params(pos, clr, prm, rgba)
+        t0 = time.perf_counter()
+        for _ in range(frames):
+            fdepth = r.foam_params(pos, clr, prm, rgba)
+        foam_ms = 1e3 * (time.perf_counter() - t0) / frames
+        foam_px = int((fdepth < 1).sum().item())
     return {"ms_per_frame": ms, "width": width, "height": height, "particles": sysm.n,
             "method": "curvature flow", "iterations": iterations, "fragments": int(frags),
             "fragments_per_s": frags / (ms / 1e3),
+            "foam_ms": foam_ms, "foam_pixels": foam_px,
             "note": "depth + thickness G-buffer in draw order, smoothing, shading; wall time "
-                    "of synchronous frames"}
+                    "of synchronous frames; foam_ms: the foam overlay (two sprites per "
+                    "particle at most, last fragment wins) over the frame, colour from one "
+                    "more step with the colour output on"}
 
 
 def workload_config(p, n=None):

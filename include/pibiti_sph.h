@@ -415,6 +415,20 @@ int sph_render_destroy(SphRenderer* renderer);
 int sph_render_frame(SphRenderer* renderer, const SphRenderParams* params, const sph_float4* pos,
                      uint32_t n, float* depth_out, float* thickness_out, sph_float4* rgba_out,
                      uint64_t* fragments);
+/* The foam overlay SetFoam draws over the shaded frame (render_particles.cpp:
+   306-334; Foam.vs, Foam.gs, Foam.fs): per particle, color[i].x is the foam
+   value w (the colour array the reference binds, aliased to the shader's
+   attribute 3); copy k = 0, 1 of the point is drawn at clip position
+   gl_Position - k when k < w, with the particle's point size; the disc is cut
+   to radius clamp(w / 0.05, 0, 1); the colour is (1, 1, 1, 1) for w >= 0.05,
+   else (1, 1, 1, 1 - w / 0.05); blending off, depth test GL_ALWAYS, so each
+   pixel keeps the last fragment in draw order.  rgba_inout (may be NULL) is
+   the frame the fragments overwrite; foam_depth_out (may be NULL) receives
+   their gl_FragDepth clamped to [0, 1], 1.0 where no foam was drawn.  Uses
+   modelview, projection, point_radius and point_scale of params; n <= 2^30.
+   Synchronous. */
+int sph_render_foam(SphRenderer* renderer, const SphRenderParams* params, const sph_float4* pos,
+                    const sph_float4* color, uint32_t n, sph_float4* rgba_inout, float* foam_depth_out);
 
 #ifdef __cplusplus
 }

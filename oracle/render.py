@@ -4,7 +4,9 @@ semantics are the reference's: Graphics/render_particles.cpp ScreenSpaceSet
 (depth test GL_LESS, blend SRC_ALPHA / ONE_MINUS_SRC_ALPHA, particles drawn
 in index order), Gbuffer.vs / Gbuffer.fs (point sprites, disc discard,
 thickness 0.02 exp(-d^2 / 6)), CurvatureFlow.fs, BilateralFilter.fs,
-ScreenSpaceRender.fs; depth textures sampled nearest with repeat wrap).
+ScreenSpaceRender.fs; depth textures sampled nearest with repeat wrap), and
+the foam overlay of SetFoam (render_particles.cpp:306-334; Foam.vs, Foam.gs,
+Foam.fs; blending off, depth test GL_ALWAYS).
 
 Single precision, with the kernel's operation order for everything up to
 the depth buffer (so depth and coverage agree bit for bit); the exponentials
@@ -39,7 +41,9 @@ def project(pos, mv, pr, W, H, radius, scale):
     ok = (cw > 0) & (np.abs(cx) <= cw) & (np.abs(cy) <= cw) & (np.abs(cz) <= cw)
     dist = np.sqrt(((ex * ex + ey * ey).astype(f32) + (ez * ez)).astype(f32)).astype(f32)
     with np.errstate(divide="ignore", invalid="ignore"):
-        size = (f32(radius) * (f32(scale) / dist).astype(f32)).astype(f32)
+        # pointRadius * (pointScale / dist) with the uniforms bound crossed
+        # (render_particles.cpp:274-275, :791-792): scale * (radius / dist)
+        size = (f32(scale) * (f32(radius) / dist).astype(f32)).astype(f32)
         size = np.minimum(np.maximum(size, f32(1)), f32(1024)).astype(f32)
         nx, ny, nz = (cx / cw).astype(f32), (cy / cw).astype(f32), (cz / cw).astype(f32)
     wx = ((nx + f32(1)).astype(f32) * f32(0.5 * W)).astype(f32)
@@ -189,3 +193,83 @@ def _shade(z, thick, mv, pr, env, bg):
     empty = (Z <= 0) | (Z == 1)
     out[empty] = [bg[0], bg[1], bg[2], 1.0]
     return out.astype(f32)
+
+
+FOAM_THRESHOLD = f32(0.05)
+
+
+def foam(pos, clr, mv, pr, W, H, radius, scale, rgba):
+    """The foam overlay over `rgba` ((H, W, 4), row 0 at the bottom):
+    returns (rgba with the foam drawn, foam depth with 1.0 where none).
+
+    Foam.vs: eye = ModelView * (x, y, z, w) with the particle's own w; the
+    size from |ModelView * (x, y, z, 1)|.  Foam.gs: copy k of the point at
+    gl_Position + vec4(-k) for every k < clr.x, at most max_vertices = 2, in
+    draw order after the particle's earlier copies.  Foam.fs: normal.xy from
+    gl_PointCoord, discard where its length d > clamp(w / 0.05, 0, 1),
+    normal.z = sqrt(1 - d), the sphere point eye + normal * r / H projected
+    and linearised with near 0.1 and far 1000; colour (1, 1, 1, 1) for
+    w >= 0.05, else (1, 1, 1, 1 - w / 0.05).  The last fragment in draw order
+    stays.  Single precision in the kernel's operation order.
+    """
+    p = np.asarray(pos, f32)
+    w = np.asarray(clr, f32)[:, 0]
+    n = len(p)
+    one = np.ones(n, f32)
+    ex, ey, ez, ew = _mul4(mv, p[:, 0], p[:, 1], p[:, 2], p[:, 3])
+    qx, qy, qz, _ = _mul4(mv, p[:, 0], p[:, 1], p[:, 2], one)
+    cx, cy, cz, cw = _mul4(pr, ex, ey, ez, ew)
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        dist = np.sqrt(((qx * qx + qy * qy).astype(f32) + (qz * qz)).astype(f32)).astype(f32)
+        r = (f32(scale) * (f32(radius) / dist).astype(f32)).astype(f32)
+        size = np.fmin(np.fmax(r, f32(1)), f32(1024)).astype(f32)  # fminf / fmaxf: NaN -> 1
+    out = np.array(rgba, f32, copy=True)
+    depth = np.ones((H, W), f32)
+    near, far = f32(0.1), f32(1000)
+    for i in range(n):
+        for k in (0, 1):
+            if not (f32(k) < w[i]):
+                continue
+            c = [f32(v + f32(-k)) for v in (cx[i], cy[i], cz[i], cw[i])]
+            if not (c[3] > 0) or abs(c[0]) > c[3] or abs(c[1]) > c[3] or abs(c[2]) > c[3]:
+                continue
+            wx = f32(f32(f32(c[0] / c[3]) + f32(1)) * f32(f32(0.5) * f32(W)))
+            wy = f32(f32(f32(c[1] / c[3]) + f32(1)) * f32(f32(0.5) * f32(H)))
+            sz = size[i]
+            h = f32(0.5) * sz
+            x0 = max(int(np.ceil(f32(f32(wx - h) - f32(0.5)))), 0)
+            x1 = min(int(np.ceil(f32(f32(wx + h) - f32(0.5)))) - 1, W - 1)
+            y0 = max(int(np.ceil(f32(f32(wy - h) - f32(0.5)))), 0)
+            y1 = min(int(np.ceil(f32(f32(wy + h) - f32(0.5)))) - 1, H - 1)
+            if x1 < x0 or y1 < y0:
+                continue
+            py, px = np.mgrid[y0:y1 + 1, x0:x1 + 1]
+            sx = (f32(0.5) + ((px.astype(f32) + f32(0.5)).astype(f32) - wx).astype(f32) / sz).astype(f32)
+            ty = (f32(0.5) - ((py.astype(f32) + f32(0.5)).astype(f32) - wy).astype(f32) / sz).astype(f32)
+            nx = ((sx - f32(0.5)).astype(f32) * f32(2)).astype(f32)
+            ny = ((ty - f32(0.5)).astype(f32) * f32(2)).astype(f32)
+            d = np.sqrt(((nx * nx).astype(f32) + (ny * ny).astype(f32)).astype(f32)).astype(f32)
+            fac = f32(min(max(f32(w[i] / FOAM_THRESHOLD), f32(0)), f32(1)))
+            keep = ~(d > fac)
+            if not keep.any():
+                continue
+            with np.errstate(invalid="ignore"):
+                nz = np.sqrt((f32(1) - d).astype(f32)).astype(f32)
+            l = np.sqrt((((nx * nx).astype(f32) + (ny * ny).astype(f32)).astype(f32)
+                         + (nz * nz).astype(f32)).astype(f32)).astype(f32)
+            ux, uy, uz = (nx / l).astype(f32), (-ny / l).astype(f32), (nz / l).astype(f32)
+            fh = f32(H)
+            fx = (ex[i] + ((ux * r[i]).astype(f32) / fh).astype(f32)).astype(f32)
+            fy = (ey[i] + ((uy * r[i]).astype(f32) / fh).astype(f32)).astype(f32)
+            fz = (ez[i] + ((uz * r[i]).astype(f32) / fh).astype(f32)).astype(f32)
+            _, _, pz, pw = _mul4(pr, fx, fy, fz, np.ones_like(fx))
+            dd = (pz / pw).astype(f32)
+            z01 = ((dd * f32(0.5)).astype(f32) + f32(0.5)).astype(f32)
+            den = (f32(far + near) - (z01 * f32(far - near)).astype(f32)).astype(f32)
+            fd = (f32(f32(2) * near) / den).astype(f32)
+            a = f32(1) if w[i] >= FOAM_THRESHOLD else f32(f32(1) - fac)
+            sub_c = out[y0:y1 + 1, x0:x1 + 1]
+            sub_d = depth[y0:y1 + 1, x0:x1 + 1]
+            sub_c[keep] = np.array([1, 1, 1, a], f32)
+            sub_d[keep] = np.fmin(np.fmax(fd, f32(0)), f32(1))[keep]
+    return out, depth

@@ -103,6 +103,7 @@ SIGNATURES = {
     "sph_render_create": [i32, i32, P(vp)],
     "sph_render_destroy": [vp],
     "sph_render_frame": [vp, vp, vp, u32, vp, vp, vp, P(ctypes.c_uint64)],
+    "sph_render_foam": [vp, vp, vp, vp, u32, vp, vp],
     "sph_scene_load_motion": [ctypes.c_char_p, i32, P(SceneMotion)],
     "sph_scene_parse_motion": [ctypes.c_char_p, P(SceneMotion)],
     "sph_emitter_particles": [P(Emitter), ctypes.c_float, vp, vp, u32, P(u32)],

@@ -21,6 +21,11 @@
 //   k_bilateral   bilateral iterations (BilateralFilter.fs), ping-pong
 //   k_shade       ScreenSpaceRender.fs: normals from depth, Fresnel,
 //                 Lambert, absorption by thickness, gamma
+// and, in sph_render_foam, the foam overlay SetFoam draws over that frame:
+//   k_foam_project  up to two foam sprites per particle (Foam.vs, Foam.gs)
+//   k_foam_cover    per covered pixel, atomicMax of the sprite's draw key
+//                   (depth test GL_ALWAYS, no blending: the last one wins)
+//   k_foam_resolve  Foam.fs for the winning sprite: colour and frag depth
 // Depth textures are sampled nearest with repeat wrap, as the reference's
 // textures are set up (render_particles.cpp:126-190, no wrap mode given).
 // The cube map and the scene behind the fluid are textures of the app; they
@@ -56,6 +61,28 @@ __device__ __forceinline__ float4 mul4(const Mat4& a, float x, float y, float z,
   return r;
 }
 
+// Point size of the sprite shaders, pointRadius * (pointScale / dist).  The
+// reference binds those uniforms crossed (render_particles.cpp:274-275 with
+// :791-792, and :326-328 with :819-820): pointRadius receives m_ParScale and
+// pointScale m_ParRadius, so the product is rounded as scale * (radius / dist).
+__device__ __forceinline__ float sprite_extent(float radius, float scale, float dist) {
+  return __fmul_rn(scale, __fdiv_rn(radius, dist));
+}
+
+// Window coordinates of a clip-space point inside the clip volume.
+__device__ __forceinline__ bool to_window(float4 c, int W, int H, float& wx, float& wy, float& wz) {
+  if (!(c.w > 0.f) || fabsf(c.x) > c.w || fabsf(c.y) > c.w || fabsf(c.z) > c.w) return false;
+  const float nx = __fdiv_rn(c.x, c.w), ny = __fdiv_rn(c.y, c.w), nz = __fdiv_rn(c.z, c.w);
+  wx = __fmul_rn(__fadd_rn(nx, 1.f), __fmul_rn(0.5f, (float)W));
+  wy = __fmul_rn(__fadd_rn(ny, 1.f), __fmul_rn(0.5f, (float)H));
+  wz = __fmul_rn(__fadd_rn(nz, 1.f), 0.5f);
+  return true;
+}
+
+__device__ __forceinline__ float norm3(float x, float y, float z) {
+  return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+}
+
 // The sprite of one particle (Gbuffer.vs): eye = MV (x, y, z, 1), clip =
 // P eye, point size from |eye|; window coordinates by the viewport
 // transform.  Points whose centre lies outside the clip volume are not drawn.
@@ -64,15 +91,8 @@ __device__ __forceinline__ Proj project(const Mat4& mv, const Mat4& pr, float4 p
   Proj o = {0.f, 0.f, 0.f, 0.f};
   const float4 e = mul4(mv, p.x, p.y, p.z, 1.f);
   const float4 c = mul4(pr, e.x, e.y, e.z, e.w);
-  if (!(c.w > 0.f) || fabsf(c.x) > c.w || fabsf(c.y) > c.w || fabsf(c.z) > c.w) return o;
-  const float dist = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(e.x, e.x), __fmul_rn(e.y, e.y)), __fmul_rn(e.z, e.z)));
-  float size = __fmul_rn(radius, __fdiv_rn(scale, dist));
-  size = fminf(fmaxf(size, 1.f), kMaxSprite);
-  const float nx = __fdiv_rn(c.x, c.w), ny = __fdiv_rn(c.y, c.w), nz = __fdiv_rn(c.z, c.w);
-  o.wx = __fmul_rn(__fadd_rn(nx, 1.f), __fmul_rn(0.5f, (float)W));
-  o.wy = __fmul_rn(__fadd_rn(ny, 1.f), __fmul_rn(0.5f, (float)H));
-  o.wz = __fmul_rn(__fadd_rn(nz, 1.f), 0.5f);
-  o.size = size;
+  if (!to_window(c, W, H, o.wx, o.wy, o.wz)) return o;
+  o.size = fminf(fmaxf(sprite_extent(radius, scale, norm3(e.x, e.y, e.z)), 1.f), kMaxSprite);
   return o;
 }
 
@@ -145,6 +165,106 @@ __global__ void k_resolve(const Proj* __restrict__ sp, const uint32_t* __restric
   }
   depth[p] = d;
   thick[p] = t;
+}
+
+// Foam overlay: Foam.vs, Foam.gs and Foam.fs as SetFoam draws them over the
+// shaded frame (render_particles.cpp:306-334).  The shader's foam value w is
+// the x of the attribute at location 3, which NVIDIA's GL driver aliases to
+// the colour array _drawPoints binds (the step's colour output).  The
+// geometry shader emits copy k of a point at gl_Position - k for each
+// k < w (max_vertices = 2, so two copies at most), both with the particle's
+// eye position and size.  Blending is off and the depth function is
+// GL_ALWAYS, so every pixel keeps the last fragment in draw order (particle,
+// then copy): the largest draw key that covers it.
+struct FoamSprite {
+  float wx, wy, size, w;  // window position, point size (0: not drawn), foam value
+  float ex, ey, ez, r;    // eyeSpacePos.xyz, eyeSpaceRadius (unclamped)
+};
+constexpr float kFoamThreshold = 0.05f;
+
+__global__ void k_foam_project(const float4* __restrict__ pos, const float4* __restrict__ clr, uint32_t n,
+                               Mat4 mv, Mat4 pr, int W, int H, float radius, float scale,
+                               FoamSprite* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = pos[i];
+  const float w = clr[i].x;
+  const float4 e = mul4(mv, p.x, p.y, p.z, p.w);  // ModelView * vPosition (the particle's own w)
+  const float4 q = mul4(mv, p.x, p.y, p.z, 1.f);  // posEye
+  const float r = sprite_extent(radius, scale, norm3(q.x, q.y, q.z));
+  const float4 c = mul4(pr, e.x, e.y, e.z, e.w);
+  for (int k = 0; k < 2; ++k) {
+    FoamSprite s = {0.f, 0.f, 0.f, w, e.x, e.y, e.z, r};
+    const float fk = -(float)k;  // gl_Position + vec4(-i)
+    float wz;
+    if ((float)k < w &&
+        to_window(make_float4(__fadd_rn(c.x, fk), __fadd_rn(c.y, fk), __fadd_rn(c.z, fk), __fadd_rn(c.w, fk)),
+                  W, H, s.wx, s.wy, wz))
+      s.size = fminf(fmaxf(r, 1.f), kMaxSprite);
+    out[2 * (size_t)i + k] = s;
+  }
+}
+
+// Foam.fs at pixel (px, py): the point coordinate's offset from the centre
+// scaled to [-1, 1] (nx, ny; origin upper left), its length d, and whether
+// the fragment survives the discard d > clamp(w / 0.05, 0, 1).
+__device__ __forceinline__ bool foam_frag(const FoamSprite& s, int px, int py, float& nx, float& ny, float& d) {
+  const float sx = __fadd_rn(0.5f, __fdiv_rn(__fsub_rn(__fadd_rn((float)px, 0.5f), s.wx), s.size));
+  const float ty = __fsub_rn(0.5f, __fdiv_rn(__fsub_rn(__fadd_rn((float)py, 0.5f), s.wy), s.size));
+  nx = __fmul_rn(__fsub_rn(sx, 0.5f), 2.f);
+  ny = __fmul_rn(__fsub_rn(ty, 0.5f), 2.f);
+  d = __fsqrt_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)));
+  return !(d > fminf(fmaxf(__fdiv_rn(s.w, kFoamThreshold), 0.f), 1.f));
+}
+
+// Per foam fragment: the pixel's draw key becomes the largest (sprite index + 1).
+__global__ void k_foam_cover(const FoamSprite* __restrict__ sp, uint32_t m, int W, int H,
+                             uint32_t* __restrict__ key) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  const FoamSprite s = sp[j];
+  if (!(s.size > 0.f)) return;
+  const Proj b = {s.wx, s.wy, 0.f, s.size};
+  int x0, x1, y0, y1;
+  sprite_box(b, W, H, x0, x1, y0, y1);
+  float nx, ny, d;
+  for (int py = y0; py <= y1; ++py)
+    for (int px = x0; px <= x1; ++px)
+      if (foam_frag(s, px, py, nx, ny, d)) atomicMax(key + (size_t)py * W + px, j + 1);
+}
+
+// The winning fragment of each pixel: colour (1, 1, 1, alpha) over the frame
+// and gl_FragDepth (the sphere point's linearised depth, near 0.1 and far
+// 1000 as Foam.fs fixes them), clamped to [0, 1] as the depth buffer stores it.
+__global__ void k_foam_resolve(const FoamSprite* __restrict__ sp, const uint32_t* __restrict__ key, int W,
+                               int H, Mat4 pr, float4* __restrict__ rgba, float* __restrict__ fdepth) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (uint32_t)(W * H)) return;
+  const uint32_t k = key[p];
+  if (k == 0) {
+    if (fdepth) fdepth[p] = 1.f;
+    return;
+  }
+  const FoamSprite s = sp[k - 1];
+  float nx, ny, d;
+  foam_frag(s, (int)(p % (uint32_t)W), (int)(p / (uint32_t)W), nx, ny, d);
+  const float nz = __fsqrt_rn(__fsub_rn(1.f, d));  // normal.z = sqrt(1 - dist), as written
+  const float l = norm3(nx, -ny, nz);
+  const float ux = __fdiv_rn(nx, l), uy = __fdiv_rn(-ny, l), uz = __fdiv_rn(nz, l);
+  const float fh = (float)H;
+  const float fx = __fadd_rn(s.ex, __fdiv_rn(__fmul_rn(ux, s.r), fh));
+  const float fy = __fadd_rn(s.ey, __fdiv_rn(__fmul_rn(uy, s.r), fh));
+  const float fz = __fadd_rn(s.ez, __fdiv_rn(__fmul_rn(uz, s.r), fh));
+  const float4 c = mul4(pr, fx, fy, fz, 1.f);
+  const float dd = __fdiv_rn(c.z, c.w);
+  const float nearp = 0.1f, farp = 1000.f;
+  const float fd = __fdiv_rn(__fmul_rn(2.f, nearp),
+                             __fsub_rn(__fadd_rn(farp, nearp),
+                                       __fmul_rn(__fadd_rn(__fmul_rn(dd, 0.5f), 0.5f), __fsub_rn(farp, nearp))));
+  const float f = fminf(fmaxf(__fdiv_rn(s.w, kFoamThreshold), 0.f), 1.f);
+  const float a = s.w >= kFoamThreshold ? 1.f : __fsub_rn(1.f, f);
+  if (rgba) rgba[p] = make_float4(1.f, 1.f, 1.f, a);
+  if (fdepth) fdepth[p] = fminf(fmaxf(fd, 0.f), 1.f);
 }
 
 // Nearest texel with repeat wrap.
@@ -376,6 +496,9 @@ struct SphRenderer {
   float *zbuf[2] = {nullptr, nullptr}, *thick = nullptr, *kern = nullptr;
   int kern_c = -1;
   uint32_t* total_host = nullptr;  // pinned
+  FoamSprite* foam = nullptr;      // two per particle
+  uint32_t foam_cap = 0;           // particles the foam sprites hold
+  uint32_t* foam_key = nullptr;    // per pixel: last foam fragment's sprite + 1
   cudaStream_t stream = nullptr;
   int sms = 1;
 };
@@ -383,7 +506,8 @@ struct SphRenderer {
 namespace {
 void render_free(SphRenderer* r) {
   void* bufs[] = {r->sprites, r->fcount, r->foff, r->cursor, r->scan_tmp, r->frag, r->scratch,
-                  r->list, r->big_list, r->counters, r->zbuf[0], r->zbuf[1], r->thick, r->kern};
+                  r->list, r->big_list, r->counters, r->zbuf[0], r->zbuf[1], r->thick, r->kern,
+                  r->foam, r->foam_key};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (r->total_host) cudaFreeHost(r->total_host);
@@ -533,6 +657,39 @@ int sph_render_frame(SphRenderer* r, const SphRenderParams* rp, const sph_float4
     SPH_CUDA(cudaMemcpyAsync(thickness_out, r->thick, sizeof(float) * P, cudaMemcpyDeviceToDevice, st), "render: thickness out");
   SPH_CUDA(cudaGetLastError(), "render: shade");
   return cuda_check(cudaStreamSynchronize(st), "render: frame");
+}
+
+int sph_render_foam(SphRenderer* r, const SphRenderParams* rp, const sph_float4* pos, const sph_float4* color,
+                    uint32_t n, sph_float4* rgba_inout, float* foam_depth_out) {
+  if (!r || !rp || ((!pos || !color) && n)) return fail(SPH_ERR_ARG, "render_foam: null argument");
+  if (n > (1u << 30)) return fail(SPH_ERR_ARG, "render_foam: %u particles (at most 2^30)", n);
+  const int W = r->W, H = r->H;
+  const size_t P = (size_t)W * H;
+  cudaStream_t st = r->stream;
+  Mat4 mv, pr;
+  for (int k = 0; k < 16; ++k) {
+    mv.m[k] = rp->modelview[k];
+    pr.m[k] = rp->projection[k];
+  }
+  if (!r->foam_key) SPH_TRY(ralloc(&r->foam_key, P, "render: foam keys"));
+  if (n > r->foam_cap) {
+    if (r->foam) cudaFree(r->foam);
+    r->foam = nullptr;
+    r->foam_cap = 0;
+    SPH_TRY(ralloc(&r->foam, 2 * (size_t)n, "render: foam sprites"));
+    r->foam_cap = n;
+  }
+  SPH_CUDA(cudaMemsetAsync(r->foam_key, 0, sizeof(uint32_t) * P, st), "render: clear foam keys");
+  if (n) {
+    k_foam_project<<<blocks_for(n), kRBlock, 0, st>>>((const float4*)pos, (const float4*)color, n, mv, pr, W, H,
+                                                      rp->point_radius, rp->point_scale, r->foam);
+    k_foam_cover<<<blocks_for(2 * (size_t)n), kRBlock, 0, st>>>(r->foam, 2 * n, W, H, r->foam_key);
+  }
+  if (rgba_inout || foam_depth_out)
+    k_foam_resolve<<<blocks_for(P), kRBlock, 0, st>>>(r->foam, r->foam_key, W, H, pr, (float4*)rgba_inout,
+                                                      foam_depth_out);
+  SPH_CUDA(cudaGetLastError(), "render: foam");
+  return cuda_check(cudaStreamSynchronize(st), "render: foam");
 }
 
 }  // extern "C"

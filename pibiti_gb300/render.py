@@ -93,12 +93,16 @@ class Renderer:
         p.background[:] = list(background)
         return p
 
-    def frame(self, pos, modelview, projection, radius: float, **kw):
+    def frame(self, pos, modelview, projection, radius: float, foam=None, **kw):
         """pos: a CUDA tensor of (n, 4) float32.  Returns (depth, thickness,
-        rgba) CUDA tensors of (H, W), (H, W), (H, W, 4), row 0 at the bottom."""
-        import torch
+        rgba) CUDA tensors of (H, W), (H, W), (H, W, 4), row 0 at the bottom.
+        foam: the particles' colours ((n, 4) float32 CUDA tensor, the step's
+        colour output); when given, the foam overlay is drawn over rgba."""
         p = self.params(modelview, projection, radius, **kw)
-        return self.frame_params(pos, p)
+        out = self.frame_params(pos, p)
+        if foam is not None:
+            self.foam_params(pos, foam, p, out[2])
+        return out
 
     def frame_params(self, pos, p: RenderParams):
         import torch
@@ -114,6 +118,21 @@ class Renderer:
                                                vp(depth), vp(thick), vp(rgba), ctypes.byref(frags)))
         self.fragments = frags.value
         return depth, thick, rgba
+
+    def foam_params(self, pos, color, p: RenderParams, rgba=None):
+        """The foam overlay (sph_render_foam): color[:, 0] of each particle
+        decides its foam sprites; rgba (an (H, W, 4) CUDA tensor, or None) is
+        overwritten where they land.  Returns their depth, (H, W), 1.0 where
+        no foam was drawn."""
+        import torch
+        if tuple(color.shape) != tuple(pos.shape):
+            raise ValueError("foam colours must have the positions' shape (n, 4)")
+        depth = torch.empty((self.height, self.width), dtype=torch.float32, device="cuda")
+        vp = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+        torch.cuda.synchronize()
+        _lib.check(_lib.lib().sph_render_foam(self._r, ctypes.c_void_p(ctypes.addressof(p)), vp(pos), vp(color),
+                                              pos.shape[0], vp(rgba), vp(depth)))
+        return depth
 
 
 def save_ppm(path: str, rgba: np.ndarray) -> None:

@@ -5,6 +5,7 @@ Depth and coverage: bit for bit (the same single-precision operations).
 Thickness: within 1e-5 relative (exp of CUDA vs NumPy).  Smoothed depth:
 within 2e-6 per curvature-flow pass and 1e-5 after the bilateral passes (the
 restatement evaluates those in double precision).  Colour: within 2e-4.
+Foam overlay (colour and depth): bit for bit.
 """
 import numpy as np
 import pytest
@@ -107,3 +108,61 @@ def test_nothing_visible(cuda):
         assert r.fragments == 0
     assert np.all(d == 1) and np.all(t == 0)
     np.testing.assert_allclose(c[..., :3], np.broadcast_to(np.array(BG, np.float32), (H, W, 3)))
+
+
+FOAM_VALUES = np.array([0.0, np.nan, -0.5, 0.01, 0.03, 0.05, 0.3, 1.0, 1.5, 3.0], np.float32)
+
+
+def _foam_scene(n=700, seed=3):
+    rng = np.random.default_rng(seed)
+    pos = np.ones((n, 4), np.float32)
+    pos[:, :3] = rng.uniform([0.0, 0.0, 0.0], [1.0, 0.7, 1.0], size=(n, 3))
+    pos[7:12, 3] = 0.5  # the foam shader's eye position uses the particle's own w
+    clr = np.zeros((n, 4), np.float32)
+    clr[:, 0] = FOAM_VALUES[rng.integers(0, len(FOAM_VALUES), n)]
+    clr[:, 1:] = rng.uniform(0, 1, (n, 3))
+    mv = look_at((0.5, 0.6, 4.0), (0.5, 0.35, 0.5))
+    pr = perspective(40.0, W / H, 0.1, 10.0)
+    return pos, clr, mv, pr
+
+
+def test_foam_overlay(cuda):
+    """sph_render_foam over a shaded frame against the restatement: every
+    foam value case (none, NaN, negative, partial disc, full disc, a second
+    copy at gl_Position - 1, more than two requested), overlapping sprites."""
+    torch = cuda
+    pos, clr, mv, pr = _foam_scene()
+    with Renderer(W, H) as r:
+        p = r.params(mv, pr, radius=0.12, env=ENV, background=BG, method=0)
+        dp = torch.from_numpy(pos).cuda()
+        _, _, rgba = r.frame_params(dp, p)
+        base = rgba.cpu().numpy()
+        fd = r.foam_params(dp, torch.from_numpy(clr).cuda(), p, rgba)
+        got, gd = rgba.cpu().numpy(), fd.cpu().numpy()
+    want, wd = orender.foam(pos, clr, mv, pr, W, H, 0.12, p.point_scale, base)
+    drawn = wd < 1
+    assert 50 < drawn.sum() < W * H - 50
+    assert np.any(drawn & (want[..., 3] > 0) & (want[..., 3] < 1))  # partial discs on top
+    np.testing.assert_array_equal(gd, wd)
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(got[~drawn], base[~drawn])
+
+
+def test_foam_none(cuda):
+    """No foam value above 0: the frame is unchanged and the foam depth is 1;
+    without a frame, only the depth is written."""
+    torch = cuda
+    pos, clr, mv, pr = _foam_scene(seed=4)
+    clr[:, 0] = 0.0
+    with Renderer(W, H) as r:
+        p = r.params(mv, pr, radius=0.12, env=ENV, background=BG, method=0)
+        dp = torch.from_numpy(pos).cuda()
+        _, _, rgba = r.frame_params(dp, p)
+        base = rgba.cpu().numpy()
+        fd = r.foam_params(dp, torch.from_numpy(clr).cuda(), p, rgba)
+        np.testing.assert_array_equal(rgba.cpu().numpy(), base)
+        assert np.all(fd.cpu().numpy() == 1)
+        clr[:, 0] = 0.5
+        fd = r.foam_params(dp, torch.from_numpy(clr).cuda(), p, None)
+    np.testing.assert_array_equal(fd.cpu().numpy(), orender.foam(pos, clr, mv, pr, W, H, 0.12, p.point_scale,
+                                                                 base)[1])
