@@ -1,5 +1,5 @@
-"""TEST INFRASTRUCTURE ONLY: the MLP corrector in NumPy, the checker of the
-GPU's tensor-core forward and backward kernels (pibiti_gb300/csrc/sph_mlp.cu).
+"""TEST INFRASTRUCTURE ONLY: the MLP corrector in NumPy, against which the
+tests compare the GPU's tensor-core forward and backward kernels (pibiti_gb300/csrc/sph_mlp.cu).
 
 Double precision, with every value the GPU holds in BF16 rounded to BF16
 at the same place: inputs, weights, hidden activations, and the output and

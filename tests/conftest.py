@@ -1,8 +1,8 @@
 """Shared test setup.
 
 Tests marked ``gpu`` need a CUDA device and the built library; everything
-else runs on the CPU.  The oracle (oracle/, the CPU restatement of the
-reference) is the checker for both.
+else runs on the CPU.  Both compare against the oracle (oracle/, the CPU
+restatement of the reference).
 """
 import os
 import sys
