@@ -87,6 +87,24 @@ def gbuffer(sprites, W, H):
     return depth, thick
 
 
+def fragment_count(sprites, W, H) -> int:
+    """Number of (pixel, sprite) fragments: pixel centres in a sprite's
+    square and inside its disc."""
+    wx, wy, wz, size = sprites
+    total = 0
+    for i in np.nonzero(size > 0)[0]:
+        h = f32(0.5) * size[i]
+        x0 = max(int(np.ceil(f32(f32(wx[i] - h) - f32(0.5)))), 0)
+        x1 = min(int(np.ceil(f32(f32(wx[i] + h) - f32(0.5)))) - 1, W - 1)
+        y0 = max(int(np.ceil(f32(f32(wy[i] - h) - f32(0.5)))), 0)
+        y1 = min(int(np.ceil(f32(f32(wy[i] + h) - f32(0.5)))) - 1, H - 1)
+        if x1 < x0 or y1 < y0:
+            continue
+        py, px = np.mgrid[y0:y1 + 1, x0:x1 + 1]
+        total += int((_mag(wx[i], wy[i], size[i], px, py) <= 1).sum())
+    return total
+
+
 def _tex(z, dx, dy):
     """z sampled at (x + dx, y + dy) with repeat wrap."""
     return np.roll(np.roll(z, -dy, axis=0), -dx, axis=1)

@@ -9,14 +9,17 @@
 //                 projection as GL column-major 4x4), clip test on the point
 //                 centre, window position and depth, sprite size
 //                 pointRadius * pointScale / |eye| (clamped to [1, 1024]);
-//                 counts the covered pixels (centre in the sprite square,
-//                 inside its disc, as Gbuffer.fs discards)
-//   scan          per-pixel fragment offsets
-//   k_emit        the particle index of each fragment into its pixel's list
-//   segment sort  each pixel's list by particle index (the GL draw order)
-//   k_resolve     per pixel, in draw order: the depth test (GL_LESS against
-//                 the cleared 1.0) and the blend SRC_ALPHA / ONE_MINUS_
-//                 SRC_ALPHA of the sprite thickness t = 0.02 exp(-d^2 / 6)
+//                 counts the sprite in each 16 x 16 pixel tile its square
+//                 reaches
+//   scan          per-tile list offsets
+//   k_bin         the particle index into each such tile's list
+//   segment sort  each tile's list by particle index (the GL draw order)
+//   k_tile_resolve one block per tile, one thread per pixel, the tile's
+//                 sprites in draw order: the covered test (centre in the
+//                 sprite square, inside its disc, as Gbuffer.fs discards),
+//                 the depth test (GL_LESS against the cleared 1.0) and the
+//                 blend SRC_ALPHA / ONE_MINUS_SRC_ALPHA of the sprite
+//                 thickness t = 0.02 exp(-d^2 / 6); counts the fragments
 //   k_curvature   curvature-flow iterations (CurvatureFlow.fs) or
 //   k_bilateral   bilateral iterations (BilateralFilter.fs), ping-pong
 //   k_shade       ScreenSpaceRender.fs: normals from depth, Fresnel,
@@ -117,54 +120,107 @@ __device__ __forceinline__ float sprite_mag(const Proj& s, int px, int py) {
   return mag > 1.f ? -1.f : mag;
 }
 
-__global__ void k_project(const float4* __restrict__ pos, uint32_t n, Mat4 mv, Mat4 pr, int W, int H,
-                          float radius, float scale, Proj* __restrict__ out,
-                          uint32_t* __restrict__ fcount) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const Proj s = project(mv, pr, pos[i], W, H, radius, scale);
-  out[i] = s;
-  if (s.size <= 0.f) return;
+constexpr int kTile = 16;                   // tile side in pixels
+constexpr int kTilePixels = kTile * kTile;  // threads of k_tile_resolve
+
+// Tiles the square of a drawn sprite reaches (false: no pixel of the image).
+__device__ __forceinline__ bool tile_range(const Proj& s, int W, int H, int& tx0, int& tx1, int& ty0,
+                                           int& ty1) {
   int x0, x1, y0, y1;
   sprite_box(s, W, H, x0, x1, y0, y1);
-  for (int py = y0; py <= y1; ++py)
-    for (int px = x0; px <= x1; ++px)
-      if (sprite_mag(s, px, py) >= 0.f) atomicAdd(fcount + (size_t)py * W + px, 1u);
+  if (x1 < x0 || y1 < y0) return false;
+  tx0 = x0 / kTile;
+  tx1 = x1 / kTile;
+  ty0 = y0 / kTile;
+  ty1 = y1 / kTile;
+  return true;
 }
 
-__global__ void k_emit(const Proj* __restrict__ sp, uint32_t n, int W, int H,
-                       uint32_t* __restrict__ cursor, uint32_t* __restrict__ frag) {
+// Sprites, per-tile sprite counts, and the number of (sprite, tile) pairs.
+__global__ void k_project(const float4* __restrict__ pos, uint32_t n, Mat4 mv, Mat4 pr, int W, int H,
+                          float radius, float scale, Proj* __restrict__ out, uint32_t* __restrict__ tcount,
+                          int TX, unsigned long long* __restrict__ pairs) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t m = 0;
+  if (i < n) {
+    const Proj s = project(mv, pr, pos[i], W, H, radius, scale);
+    out[i] = s;
+    int tx0, tx1, ty0, ty1;
+    if (s.size > 0.f && tile_range(s, W, H, tx0, tx1, ty0, ty1)) {
+      for (int ty = ty0; ty <= ty1; ++ty)
+        for (int tx = tx0; tx <= tx1; ++tx) atomicAdd(tcount + ty * TX + tx, 1u);
+      m = (uint32_t)((tx1 - tx0 + 1) * (ty1 - ty0 + 1));
+    }
+  }
+  const uint32_t wm = __reduce_add_sync(0xffffffffu, m);  // <= 32 x 66 x 66
+  if ((threadIdx.x & 31) == 0 && wm) atomicAdd(pairs, (unsigned long long)wm);
+}
+
+// The particle index into the list of every tile its sprite reaches.
+__global__ void k_bin(const Proj* __restrict__ sp, uint32_t n, int W, int H, int TX,
+                      uint32_t* __restrict__ cursor, uint32_t* __restrict__ tlist) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Proj s = sp[i];
-  if (s.size <= 0.f) return;
-  int x0, x1, y0, y1;
-  sprite_box(s, W, H, x0, x1, y0, y1);
-  for (int py = y0; py <= y1; ++py)
-    for (int px = x0; px <= x1; ++px)
-      if (sprite_mag(s, px, py) >= 0.f) frag[atomicAdd(cursor + (size_t)py * W + px, 1u)] = i;
+  int tx0, tx1, ty0, ty1;
+  if (!(s.size > 0.f) || !tile_range(s, W, H, tx0, tx1, ty0, ty1)) return;
+  for (int ty = ty0; ty <= ty1; ++ty)
+    for (int tx = tx0; tx <= tx1; ++tx) tlist[atomicAdd(cursor + ty * TX + tx, 1u)] = i;
 }
 
-// Depth test and blend in draw order (the list is sorted by particle index).
-__global__ void k_resolve(const Proj* __restrict__ sp, const uint32_t* __restrict__ frag,
-                          const uint32_t* __restrict__ foff, const uint32_t* __restrict__ fcount,
-                          int W, int H, float* __restrict__ depth, float* __restrict__ thick) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= (uint32_t)(W * H)) return;
-  const int px = (int)(p % (uint32_t)W), py = (int)(p / (uint32_t)W);
-  float d = 1.f, t = 0.f;
-  const uint32_t s0 = foff[p], n = fcount[p];
-  for (uint32_t k = 0; k < n; ++k) {
-    const Proj s = sp[frag[s0 + k]];
-    if (s.wz < d) {
+struct BoxedSprite {
+  float wx, wy, wz, size;
+  int x0, x1, y0, y1;  // sprite_box
+};
+
+// One block per tile, one thread per pixel: the tile's sprites (sorted by
+// particle index) in chunks through shared memory; per pixel, in draw order,
+// the covered test, the depth test and the blend.  Adds the covered
+// fragments to *frags.
+__global__ void __launch_bounds__(kTilePixels)
+k_tile_resolve(const Proj* __restrict__ sp, const uint32_t* __restrict__ tlist,
+               const uint32_t* __restrict__ toff, const uint32_t* __restrict__ tcount, int W, int H, int TX,
+               float* __restrict__ depth, float* __restrict__ thick, unsigned long long* __restrict__ frags) {
+  __shared__ BoxedSprite sb[kTilePixels];
+  const uint32_t t = blockIdx.x;
+  const int px = (int)(t % (uint32_t)TX) * kTile + (int)(threadIdx.x % kTile);
+  const int py = (int)(t / (uint32_t)TX) * kTile + (int)(threadIdx.x / kTile);
+  const bool valid = px < W && py < H;
+  const uint32_t s0 = toff[t], n = tcount[t];
+  float d = 1.f, th = 0.f;
+  uint32_t covered = 0;
+  for (uint32_t c0 = 0; c0 < n; c0 += kTilePixels) {
+    const uint32_t m = min(n - c0, (uint32_t)kTilePixels);
+    __syncthreads();  // the previous chunk is consumed
+    if (threadIdx.x < m) {
+      const Proj s = sp[tlist[s0 + c0 + threadIdx.x]];
+      BoxedSprite b = {s.wx, s.wy, s.wz, s.size, 0, -1, 0, -1};
+      sprite_box(s, W, H, b.x0, b.x1, b.y0, b.y1);
+      sb[threadIdx.x] = b;
+    }
+    __syncthreads();
+    if (!valid) continue;
+    for (uint32_t k = 0; k < m; ++k) {
+      const BoxedSprite b = sb[k];
+      if (px < b.x0 || px > b.x1 || py < b.y0 || py > b.y1) continue;
+      const Proj s = {b.wx, b.wy, b.wz, b.size};
       const float mag = sprite_mag(s, px, py);
-      const float tv = __fmul_rn(0.02f, expf(__fdiv_rn(-mag, 6.f)));
-      d = s.wz;
-      t = __fadd_rn(__fmul_rn(tv, tv), __fmul_rn(t, __fsub_rn(1.f, tv)));
+      if (mag < 0.f) continue;
+      ++covered;
+      if (s.wz < d) {
+        const float tv = __fmul_rn(0.02f, expf(__fdiv_rn(-mag, 6.f)));
+        d = s.wz;
+        th = __fadd_rn(__fmul_rn(tv, tv), __fmul_rn(th, __fsub_rn(1.f, tv)));
+      }
     }
   }
-  depth[p] = d;
-  thick[p] = t;
+  if (valid) {
+    depth[(size_t)py * W + px] = d;
+    thick[(size_t)py * W + px] = th;
+  }
+  unsigned long long c = covered;
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(frags, c);
 }
 
 // Foam overlay: Foam.vs, Foam.gs and Foam.fs as SetFoam draws them over the
@@ -488,14 +544,18 @@ struct SphRenderer {
   int W = 0, H = 0;
   uint32_t nparticles = 0;  // capacity of the sprite array
   Proj* sprites = nullptr;
-  uint32_t *fcount = nullptr, *foff = nullptr, *cursor = nullptr, *scan_tmp = nullptr;
-  uint32_t* frag = nullptr;  // fragment particle indices
-  uint32_t* scratch = nullptr;
-  size_t frag_cap = 0;
-  uint32_t *list = nullptr, *big_list = nullptr, *counters = nullptr;
+  int TX = 0, TY = 0;  // tiles of kTile x kTile pixels
+  uint32_t T = 0;
+  uint32_t *tcount = nullptr, *toff = nullptr, *tcursor = nullptr, *scan_tmp = nullptr;
+  uint32_t* tlist = nullptr;     // per tile: particle indices of the sprites that reach it
+  uint32_t* tscratch = nullptr;  // 2 words per list entry (long-list sorts)
+  size_t tlist_cap = 0;
+  uint32_t *tsort = nullptr, *tbig = nullptr, *counters = nullptr;
+  unsigned long long* dcount = nullptr;  // (sprite, tile) pairs, covered fragments
   float *zbuf[2] = {nullptr, nullptr}, *thick = nullptr, *kern = nullptr;
   int kern_c = -1;
-  uint32_t* total_host = nullptr;  // pinned
+  uint32_t* total_host = nullptr;         // pinned: list entries
+  unsigned long long* hcount = nullptr;   // pinned: dcount
   FoamSprite* foam = nullptr;      // two per particle
   uint32_t foam_cap = 0;           // particles the foam sprites hold
   uint32_t* foam_key = nullptr;    // per pixel: last foam fragment's sprite + 1
@@ -505,12 +565,13 @@ struct SphRenderer {
 
 namespace {
 void render_free(SphRenderer* r) {
-  void* bufs[] = {r->sprites, r->fcount, r->foff, r->cursor, r->scan_tmp, r->frag, r->scratch,
-                  r->list, r->big_list, r->counters, r->zbuf[0], r->zbuf[1], r->thick, r->kern,
+  void* bufs[] = {r->sprites, r->tcount, r->toff, r->tcursor, r->scan_tmp, r->tlist, r->tscratch,
+                  r->tsort, r->tbig, r->counters, r->dcount, r->zbuf[0], r->zbuf[1], r->thick, r->kern,
                   r->foam, r->foam_key};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (r->total_host) cudaFreeHost(r->total_host);
+  if (r->hcount) cudaFreeHost(r->hcount);
 }
 template <class T>
 int ralloc(T** p, size_t n, const char* what) {
@@ -528,18 +589,25 @@ int sph_render_create(int width, int height, SphRenderer** out) {
   r->W = width;
   r->H = height;
   const size_t P = (size_t)width * height;
+  r->TX = (width + kTile - 1) / kTile;
+  r->TY = (height + kTile - 1) / kTile;
+  r->T = (uint32_t)r->TX * (uint32_t)r->TY;
+  const size_t T = r->T;
   int rc = SPH_OK;
-  if (rc == SPH_OK) rc = ralloc(&r->fcount, P + 1, "render: fragment counts");
-  if (rc == SPH_OK) rc = ralloc(&r->foff, P + 1, "render: fragment offsets");
-  if (rc == SPH_OK) rc = ralloc(&r->cursor, P, "render: fragment cursors");
-  if (rc == SPH_OK) rc = ralloc(&r->scan_tmp, scan_scratch_words((uint32_t)(P + 1)), "render: scan scratch");
-  if (rc == SPH_OK) rc = ralloc(&r->list, P, "render: sort list");  // every pixel may need a sort
-  if (rc == SPH_OK) rc = ralloc(&r->big_list, P, "render: big sort list");
+  if (rc == SPH_OK) rc = ralloc(&r->tcount, T + 1, "render: tile counts");
+  if (rc == SPH_OK) rc = ralloc(&r->toff, T + 1, "render: tile offsets");
+  if (rc == SPH_OK) rc = ralloc(&r->tcursor, T, "render: tile cursors");
+  if (rc == SPH_OK) rc = ralloc(&r->scan_tmp, scan_scratch_words((uint32_t)(T + 1)), "render: scan scratch");
+  if (rc == SPH_OK) rc = ralloc(&r->tsort, T, "render: sort list");  // every tile may need a sort
+  if (rc == SPH_OK) rc = ralloc(&r->tbig, T, "render: long sort list");
   if (rc == SPH_OK) rc = ralloc(&r->counters, 2, "render: sort counters");
+  if (rc == SPH_OK) rc = ralloc(&r->dcount, 2, "render: pair and fragment counts");
   if (rc == SPH_OK) rc = ralloc(&r->zbuf[0], P, "render: depth");
   if (rc == SPH_OK) rc = ralloc(&r->zbuf[1], P, "render: depth");
   if (rc == SPH_OK) rc = ralloc(&r->thick, P, "render: thickness");
   if (rc == SPH_OK) rc = cuda_check(cudaMallocHost((void**)&r->total_host, sizeof(uint32_t)), "render: host word");
+  if (rc == SPH_OK)
+    rc = cuda_check(cudaMallocHost((void**)&r->hcount, 2 * sizeof(unsigned long long)), "render: host counts");
   if (rc == SPH_OK) rc = cuda_check(cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking), "render: stream");
   if (rc == SPH_OK)
     rc = cuda_check(cudaFuncSetAttribute(k_sort_big_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -598,36 +666,42 @@ int sph_render_frame(SphRenderer* r, const SphRenderParams* rp, const sph_float4
     SPH_TRY(ralloc(&r->sprites, n, "render: sprites"));
     r->nparticles = n;
   }
-  // G-buffer: count, scan, emit, sort each pixel's list, resolve
-  SPH_CUDA(cudaMemsetAsync(r->fcount, 0, sizeof(uint32_t) * (P + 1), st), "render: clear counts");
+  // G-buffer: sprites and tile counts, scan, bin, sort each tile's list, resolve
+  const uint32_t T = r->T;
+  SPH_CUDA(cudaMemsetAsync(r->tcount, 0, sizeof(uint32_t) * (T + 1), st), "render: clear tile counts");
+  SPH_CUDA(cudaMemsetAsync(r->dcount, 0, 2 * sizeof(unsigned long long), st), "render: clear counts");
   if (n)
     k_project<<<blocks_for(n), kRBlock, 0, st>>>((const float4*)pos, n, mv, pr, W, H, rp->point_radius,
-                                                 rp->point_scale, r->sprites, r->fcount);
+                                                 rp->point_scale, r->sprites, r->tcount, r->TX, r->dcount);
   SPH_CUDA(cudaGetLastError(), "render: project");
-  SPH_TRY(exclusive_scan(r->fcount, r->foff, (uint32_t)(P + 1), r->scan_tmp, st));
-  SPH_CUDA(cudaMemcpyAsync(r->total_host, r->foff + P, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "render: total");
+  SPH_TRY(exclusive_scan(r->tcount, r->toff, T + 1, r->scan_tmp, st));
+  SPH_CUDA(cudaMemcpyAsync(r->total_host, r->toff + T, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "render: total");
+  SPH_CUDA(cudaMemcpyAsync(r->hcount, r->dcount, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st),
+           "render: pairs");
   SPH_CUDA(cudaStreamSynchronize(st), "render: total");
-  const size_t F = *r->total_host;
-  if (fragments) *fragments = F;
-  if (F > r->frag_cap) {
-    if (r->frag) cudaFree(r->frag);
-    if (r->scratch) cudaFree(r->scratch);
-    r->frag = r->scratch = nullptr;
-    r->frag_cap = 0;
-    SPH_TRY(ralloc(&r->frag, F, "render: fragments"));
-    SPH_TRY(ralloc(&r->scratch, 2 * F, "render: sort scratch"));
-    r->frag_cap = F;
+  if (r->hcount[0] >= (1ull << 32))
+    return fail(SPH_ERR_ARG, "render_frame: %llu sprite-tile pairs (at most 2^32 - 1)", r->hcount[0]);
+  const size_t M = *r->total_host;
+  if (M > r->tlist_cap) {
+    if (r->tlist) cudaFree(r->tlist);
+    if (r->tscratch) cudaFree(r->tscratch);
+    r->tlist = r->tscratch = nullptr;
+    r->tlist_cap = 0;
+    SPH_TRY(ralloc(&r->tlist, M, "render: tile lists"));
+    SPH_TRY(ralloc(&r->tscratch, 2 * M, "render: sort scratch"));
+    r->tlist_cap = M;
   }
-  if (F) {
-    SPH_CUDA(cudaMemcpyAsync(r->cursor, r->foff, sizeof(uint32_t) * P, cudaMemcpyDeviceToDevice, st), "render: cursors");
-    k_emit<<<blocks_for(n), kRBlock, 0, st>>>(r->sprites, n, W, H, r->cursor, r->frag);
+  if (M) {
+    SPH_CUDA(cudaMemcpyAsync(r->tcursor, r->toff, sizeof(uint32_t) * T, cudaMemcpyDeviceToDevice, st), "render: cursors");
+    k_bin<<<blocks_for(n), kRBlock, 0, st>>>(r->sprites, n, W, H, r->TX, r->tcursor, r->tlist);
     SPH_CUDA(cudaMemsetAsync(r->counters, 0, 2 * sizeof(uint32_t), st), "render: sort counters");
-    k_find_cells<<<blocks_for(P), kRBlock, 0, st>>>((uint32_t)P, r->fcount, 1u, r->list, r->counters, r->big_list);
-    k_sort_cells<<<8 * r->sms, kSortWarps * 32, 0, st>>>(r->foff, r->fcount, r->frag, r->list, r->counters);
+    k_find_cells<<<blocks_for(T), kRBlock, 0, st>>>(T, r->tcount, 1u, r->tsort, r->counters, r->tbig);
+    k_sort_cells<<<8 * r->sms, kSortWarps * 32, 0, st>>>(r->toff, r->tcount, r->tlist, r->tsort, r->counters);
     k_sort_big_cells<<<r->sms, kBigThreads, kBlockSortMax * sizeof(uint32_t), st>>>(
-        r->foff, r->fcount, r->frag, r->big_list, r->counters + 1, r->scratch);
+        r->toff, r->tcount, r->tlist, r->tbig, r->counters + 1, r->tscratch);
   }
-  k_resolve<<<blocks_for(P), kRBlock, 0, st>>>(r->sprites, r->frag, r->foff, r->fcount, W, H, r->zbuf[0], r->thick);
+  k_tile_resolve<<<T, kTilePixels, 0, st>>>(r->sprites, r->tlist, r->toff, r->tcount, W, H, r->TX, r->zbuf[0],
+                                            r->thick, r->dcount + 1);
   SPH_CUDA(cudaGetLastError(), "render: g-buffer");
   // smoothing
   int cur = 0;
@@ -656,7 +730,11 @@ int sph_render_frame(SphRenderer* r, const SphRenderParams* rp, const sph_float4
   if (thickness_out)
     SPH_CUDA(cudaMemcpyAsync(thickness_out, r->thick, sizeof(float) * P, cudaMemcpyDeviceToDevice, st), "render: thickness out");
   SPH_CUDA(cudaGetLastError(), "render: shade");
-  return cuda_check(cudaStreamSynchronize(st), "render: frame");
+  SPH_CUDA(cudaMemcpyAsync(r->hcount + 1, r->dcount + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st),
+           "render: fragments");
+  SPH_TRY(cuda_check(cudaStreamSynchronize(st), "render: frame"));
+  if (fragments) *fragments = r->hcount[1];
+  return SPH_OK;
 }
 
 int sph_render_foam(SphRenderer* r, const SphRenderParams* rp, const sph_float4* pos, const sph_float4* color,

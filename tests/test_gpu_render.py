@@ -30,24 +30,49 @@ def _scene(n=400, seed=0):
     return pos, mv, pr
 
 
-def _frame(torch, pos, mv, pr, **kw):
-    with Renderer(W, H) as r:
+def _frame(torch, pos, mv, pr, w=W, h=H, **kw):
+    with Renderer(w, h) as r:
         p = r.params(mv, pr, radius=0.03, env=ENV, background=BG, **kw)
         d, t, c = r.frame_params(torch.from_numpy(pos).cuda(), p)
         frags = r.fragments
     return d.cpu().numpy(), t.cpu().numpy(), c.cpu().numpy(), p, frags
 
 
-def test_gbuffer_and_shading(cuda):
+@pytest.mark.parametrize("w,h", [(W, H), (101, 70)])  # 101 x 70: partial 16 x 16 tiles
+def test_gbuffer_and_shading(cuda, w, h):
     pos, mv, pr = _scene()
-    d, t, c, p, frags = _frame(cuda, pos, mv, pr, method=0)
-    sprites = orender.project(pos, mv, pr, W, H, 0.03, p.point_scale)
-    od, ot = orender.gbuffer(sprites, W, H)
-    assert (od < 1).sum() > W * H // 20
+    pr = perspective(50.0, w / h, 0.1, 10.0)
+    d, t, c, p, frags = _frame(cuda, pos, mv, pr, w, h, method=0)
+    sprites = orender.project(pos, mv, pr, w, h, 0.03, p.point_scale)
+    od, ot = orender.gbuffer(sprites, w, h)
+    assert (od < 1).sum() > w * h // 20
     assert frags > (od < 1).sum()  # overlapping sprites
+    assert frags == orender.fragment_count(sprites, w, h)
     np.testing.assert_array_equal(d, od)
     np.testing.assert_allclose(t, ot, rtol=1e-5, atol=1e-9)
     np.testing.assert_allclose(c, orender.shade(od, ot, mv, pr, ENV, BG), rtol=0, atol=2e-4)
+
+
+def test_crowded_tiles(cuda):
+    """Tile lists past the warp-sort (1024) and the shared-memory-sort
+    (16384) limits: 30,000 sprites of 6-9 px over a 64 x 48 image, about
+    20,000 in each of the two middle tiles."""
+    torch = cuda
+    rng = np.random.default_rng(5)
+    n = 30000
+    pos = np.ones((n, 4), np.float32)
+    pos[:, :3] = rng.uniform([0.3, 0.2, 0.3], [0.7, 0.5, 0.7], size=(n, 3))
+    mv = look_at((0.5, 0.35, 1.6), (0.5, 0.35, 0.5))
+    pr = perspective(50.0, 64 / 48, 0.1, 10.0)
+    with Renderer(64, 48) as r:
+        p = r.params(mv, pr, radius=0.1, method=0)
+        d, t, _ = (x.cpu().numpy() for x in r.frame_params(torch.from_numpy(pos).cuda(), p))
+        frags = r.fragments
+    sprites = orender.project(pos, mv, pr, 64, 48, 0.1, p.point_scale)
+    od, ot = orender.gbuffer(sprites, 64, 48)
+    assert frags == orender.fragment_count(sprites, 64, 48)
+    np.testing.assert_array_equal(d, od)
+    np.testing.assert_allclose(t, ot, rtol=1e-5, atol=1e-9)
 
 
 @pytest.mark.parametrize("iters", [1, 6])
