@@ -1,6 +1,6 @@
 // sph_segsort.cuh -- sorting many independent segments of uint32 keys
 // (segment k: data[start[k], start[k] + count[k])), used for the ids of
-// crowded grid cells and for the per-pixel fragment lists of the renderer.
+// crowded grid cells and for the renderer's per-tile sprite lists.
 // Three kernels:
 //   k_find_cells      segments longer than `min_sort` go to `list` (up to
 //                     kWarpSortMax) or `big_list`, one atomic per warp and list
