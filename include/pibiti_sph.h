@@ -411,7 +411,8 @@ int sph_render_destroy(SphRenderer* renderer);
    width x height, row 0 at the bottom as GL's window coordinates; any may
    be NULL): the smoothed depth (1.0 where nothing was drawn), the
    thickness, the RGBA image.  *fragments (may be NULL) receives the number
-   of sprite fragments.  Synchronous. */
+   of sprite fragments.  A frame whose sprites reach 2^32 or more (sprite,
+   16 x 16 pixel tile) pairs is refused with SPH_ERR_ARG.  Synchronous. */
 int sph_render_frame(SphRenderer* renderer, const SphRenderParams* params, const sph_float4* pos,
                      uint32_t n, float* depth_out, float* thickness_out, sph_float4* rgba_out,
                      uint64_t* fragments);
