@@ -27,6 +27,7 @@ import math
 
 import numpy as np
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -175,6 +176,31 @@ def time_cpu_oracle(budget_s: float, min_steps: int = 3):
         t += time.perf_counter() - t0
         steps += 1
     return w.n * steps / t, steps, oracle.threads(), w.n
+
+
+def run_cpu_configs(args) -> int:
+    """The oracle's single-precision step (OpenMP, all host threads) on the
+    full workloads, one JSON line each: the 32,768-particle dam break, the
+    1,048,576-particle double dam break and, with fewer steps, the
+    16,777,216-particle uniform block.  One untimed step first."""
+    import oracle
+    from pibiti_gb300 import configs
+    from pibiti_gb300.sph import Scene
+    cases = (("dam break, 32,768 particles", configs.dambreak_small, 100),
+             ("double dam break, 1,048,576 particles", configs.dambreak_double, 5),
+             ("uniform block, 16,777,216 particles", configs.uniform_stress, 2))
+    for name, make, k in cases:
+        w = make()
+        p = Scene.parse(w.xml).params
+        pos, vel = oracle.step(p, w.pos, w.vel, steps=1)
+        t0 = time.perf_counter()
+        pos, vel = oracle.step(p, pos, vel, steps=k)
+        t = time.perf_counter() - t0
+        print(json.dumps({"impl": "reference", "kind": "port", "workload": name, "particles": w.n,
+                          "steps": k, "value": w.n * k / t, "unit": UNIT, "ms_per_step": 1e3 * t / k,
+                          "cores": oracle.threads(), "cpu": platform.machine()}), flush=True)
+        del w, pos, vel
+    return 0
 
 
 def run_reference(args):
@@ -471,8 +497,12 @@ def main():
                     help="profiling aid: run --warm-steps steps of the workload, save the state, exit")
     ap.add_argument("--stages", metavar="NPZ",
                     help="profiling aid: load a saved state, print --steps per-stage step times")
+    ap.add_argument("--cpu-configs", action="store_true",
+                    help="time the oracle's CPU step on the full 32K, 1M and 16.7M workloads and exit")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.cpu_configs:
+        return run_cpu_configs(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.save_state or args.stages:
