@@ -79,6 +79,33 @@ def job_throughput(particles_per_rank: int, steps: int, world: int, max_ms: floa
     return world * particles_per_rank * steps / (max_ms / 1e3)
 
 
+def shard_scenes(sizes, world: int, rank: int) -> list:
+    """Scenes of `rank` when the ensemble's independent scenes are split over
+    `world` GPUs: largest first to the least-loaded rank (ties to the lower
+    rank), so the ranks' particle totals differ by at most one scene.  The
+    same plan on every rank; returned in scene order."""
+    load = [0] * world
+    owner = [0] * len(sizes)
+    for k in sorted(range(len(sizes)), key=lambda q: (-sizes[q], q)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        owner[k] = r
+        load[r] += sizes[k]
+    return [k for k in range(len(sizes)) if owner[k] == rank]
+
+
+def barrier() -> None:
+    """All ranks meet (no-op without a process group)."""
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+def ensemble_throughput(total_particles: int, steps: int, max_ms: float) -> float:
+    """Whole-job particle-steps/s of the sharded ensemble: every scene of the
+    job over the slowest rank's time."""
+    return total_particles * steps / (max_ms / 1e3)
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -246,8 +273,19 @@ def run_ensemble(args):
     import torch
     from pibiti_gb300 import configs
     from pibiti_gb300.sph import ARRAY_POS, ARRAY_VEL, SPH, Scene
-    torch.cuda.set_device(0)
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     e = configs.ensemble(steps=args.steps)
+    total = e.n
+    if world > 1:  # independent scenes: each rank steps its share, no exchange
+        mine = shard_scenes(e.sizes, world, rank)
+        offs = np.concatenate([[0], np.cumsum(e.sizes)])
+        sel = np.concatenate([np.arange(offs[k], offs[k + 1]) for k in mine])
+        e = configs.Ensemble(e.name, [e.xmls[k] for k in mine], e.pos[sel], e.vel[sel],
+                             [e.sizes[k] for k in mine], e.steps, dict(e.notes, scenes=mine))
     ps = [Scene.parse(x).params for x in e.xmls]
     stream = torch.cuda.Stream()
     sysm = SPH(ps, stream=stream)
@@ -259,19 +297,33 @@ def run_ensemble(args):
     sysm.set_graph_steps(steps)
     sysm.update(steps)  # builds and runs the graph once (untimed)
     torch.cuda.synchronize()
-    clocks = ClockSampler(0)
+    clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
+    barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     sysm.update(steps)  # one graph launch
     e1.record(stream)
     torch.cuda.synchronize()
+    barrier()
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    value = sysm.n * steps / (ms / 1e3)
+    ms = max_over_ranks(e0.elapsed_time(e1), device="cuda")
+    value = ensemble_throughput(total, steps, ms)
     st = sysm.stats()
     sysm.close()
+    if world > 1:  # the single-GPU comparisons below are not repeated per rank
+        if rank == 0:
+            print(json.dumps({
+                "metric": "ensemble particle-steps/s", "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps,
+                "higher_is_better": True, "scaling": "strong", "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "batched ensemble: 256 dam-break scenes split over the GPUs by "
+                                       "particle count (no exchange)", "particles": total,
+                           "graph": f"{steps} steps captured as one CUDA graph per rank"},
+                "clocks": clk}), flush=True)
+        torch.distributed.destroy_process_group()
+        return 0
     # the same steps as one persistent cooperative launch, from the same start
     with SPH(ps, stream=stream) as ph:
         ph.set_array(ARRAY_POS, e.pos)
