@@ -19,7 +19,38 @@ from . import _lib
 from ._lib import ARRAY_POS, ARRAY_VEL, SceneInfo, SceneMotion, check, lib
 from .params import SimParams
 
-__all__ = ["Scene", "SPH", "ARRAY_POS", "ARRAY_VEL", "stage"]
+__all__ = ["Scene", "SPH", "ARRAY_POS", "ARRAY_VEL", "stage", "write_snapshot", "read_snapshot"]
+
+SNAPSHOT_VERSION = 1
+
+
+def write_snapshot(path: str, params: Sequence[SimParams], offsets, pos, vel, step: int = 0,
+                   extra: Optional[dict] = None) -> None:
+    """A checkpoint file (.npz): every scene's SimParams bytes, the scene
+    offsets, positions and velocities in original particle order (float4),
+    the caller's step count and any extra arrays of the caller (dye, emitter
+    index, ...).  The reference keeps no state beyond these (its only state
+    I/O is getArray / setArray, SPH_Util.cpp:44-71)."""
+    raw = np.stack([np.frombuffer(p.to_bytes(), np.uint8) for p in params])
+    arrays = {"extra_" + k: np.asarray(v) for k, v in (extra or {}).items()}
+    np.savez(path, version=np.int64(SNAPSHOT_VERSION), params=raw, offsets=np.asarray(offsets, np.int64),
+             pos=np.asarray(pos, np.float32).reshape(-1, 4), vel=np.asarray(vel, np.float32).reshape(-1, 4),
+             step=np.int64(step), **arrays)
+
+
+def read_snapshot(path: str) -> dict:
+    """The contents of a write_snapshot file: params (list of SimParams),
+    offsets, pos, vel, step, extra (dict)."""
+    with np.load(path) as d:
+        if int(d["version"]) != SNAPSHOT_VERSION:
+            raise ValueError(f"{path}: snapshot version {int(d['version'])}, expected {SNAPSHOT_VERSION}")
+        out = dict(params=[SimParams.from_bytes(row.tobytes()) for row in d["params"]],
+                   offsets=[int(v) for v in d["offsets"]], pos=d["pos"].copy(), vel=d["vel"].copy(),
+                   step=int(d["step"]),
+                   extra={k[len("extra_"):]: d[k].copy() for k in d.files if k.startswith("extra_")})
+    if out["offsets"][-1] != len(out["pos"]) or len(out["pos"]) != len(out["vel"]):
+        raise ValueError(f"{path}: particle count does not match the scene offsets")
+    return out
 
 
 def _is_torch(x) -> bool:
@@ -195,6 +226,29 @@ class SPH:
         ptr, dev, keep = _buf(out)
         check(lib().sph_get_array(self._h, which, ptr, int(dev)))
         return out
+
+    def snapshot(self, path: str, step: int = 0, extra: Optional[dict] = None) -> None:
+        """Checkpoint: the scenes' current SimParams, positions and velocities
+        (write_snapshot).  restore() continues the plain step bit for bit;
+        the learned step restarts its density history."""
+        write_snapshot(path, [self.params(k) for k in range(self.num_scenes)], self.offsets,
+                       self.get_array(ARRAY_POS), self.get_array(ARRAY_VEL), step, extra)
+
+    @classmethod
+    def restore(cls, path: str, stream=None):
+        """A new handle from a snapshot file: (handle, step, extra)."""
+        snap = read_snapshot(path)
+        ps = snap["params"]
+        s = cls(ps[0] if len(ps) == 1 else ps, stream=stream)
+        try:
+            if list(s.offsets) != snap["offsets"]:
+                raise ValueError(f"{path}: scene sizes differ from the parameters' particle counts")
+            s.set_array(ARRAY_POS, snap["pos"])
+            s.set_array(ARRAY_VEL, snap["vel"])
+        except Exception:
+            s.close()
+            raise
+        return s, snap["step"], snap["extra"]
 
     def emit(self, pos, vel, emit_id: int) -> int:
         """Writes emitted particles at the running emit index (App::emitId,
