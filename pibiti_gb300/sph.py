@@ -33,6 +33,9 @@ def write_snapshot(path: str, params: Sequence[SimParams], offsets, pos, vel, st
     I/O is getArray / setArray, SPH_Util.cpp:44-71)."""
     raw = np.stack([np.frombuffer(p.to_bytes(), np.uint8) for p in params])
     arrays = {"extra_" + k: np.asarray(v) for k, v in (extra or {}).items()}
+    for k, v in arrays.items():
+        if v.dtype == object:
+            raise TypeError(f"snapshot extra {k[len('extra_'):]!r}: numeric arrays only")
     np.savez(path, version=np.int64(SNAPSHOT_VERSION), params=raw, offsets=np.asarray(offsets, np.int64),
              pos=np.asarray(pos, np.float32).reshape(-1, 4), vel=np.asarray(vel, np.float32).reshape(-1, 4),
              step=np.int64(step), **arrays)

@@ -44,3 +44,9 @@ def test_inconsistent_files_refused(tmp_path):
     np.savez(path, **items)
     with pytest.raises(ValueError, match="version"):
         read_snapshot(path)
+
+
+def test_object_extras_refused(tmp_path):
+    ps, offs, pos, vel = _scenes()
+    with pytest.raises(TypeError, match="numeric"):
+        write_snapshot(str(tmp_path / "s.npz"), ps, offs, pos, vel, extra={"bad": [object()]})
