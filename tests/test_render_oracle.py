@@ -106,3 +106,29 @@ def test_fragment_depth():
         zn = f[2] / f[3]
         want = 0.2 / (1000.1 - (zn * 0.5 + 0.5) * 999.9)
         np.testing.assert_allclose(d[y, x], want, rtol=2e-5)
+
+
+def test_sprite_size_rounding_order():
+    """The sprite shaders compute pointRadius * (pointScale / dist) with the
+    uniforms bound crossed (pointRadius = m_ParScale, pointScale =
+    m_ParRadius, render_particles.cpp:274-275, :791-792): the size rounds
+    as scale * (radius / dist), which differs from radius * (scale / dist)
+    in the last bit for some distances."""
+    f32 = np.float32
+    mv = np.eye(4, dtype=np.float32).ravel()
+    mv[14] = -2.0  # camera 2 units in front of the particles
+    pr = perspective(60.0, 1.0, 0.1, 10.0)
+    rng = np.random.default_rng(3)
+    pos = np.ones((4000, 4), np.float32)
+    pos[:, :2] = rng.uniform(-0.3, 0.3, (4000, 2))
+    pos[:, 2] = rng.uniform(-0.5, 0.5, 4000)
+    radius, scale = 0.0173, 93.7
+    _, _, _, size = orender.project(pos, mv, pr, 256, 256, radius, scale)
+    ex, ey, ez = pos[:, 0], pos[:, 1], (pos[:, 2] + f32(-2.0)).astype(f32)
+    dist = np.sqrt(((ex * ex + ey * ey).astype(f32) + (ez * ez)).astype(f32)).astype(f32)
+    ref = (f32(scale) * (f32(radius) / dist).astype(f32)).astype(f32)
+    other = (f32(radius) * (f32(scale) / dist).astype(f32)).astype(f32)
+    drawn = size > 0
+    assert drawn.sum() > 3000
+    np.testing.assert_array_equal(size[drawn], np.clip(ref, 1, 1024)[drawn])
+    assert np.any(ref[drawn] != other[drawn])
