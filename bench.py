@@ -7,17 +7,23 @@ double dam break, with the HBM roofline of the dominant kernel.
 One step is one cSPH::Update (integrate, hash, sort, cell ranges, density,
 force) over all particles.  Inputs are synthetic and seeded
 (pibiti_gb300/configs.py).  Our arm times K steps with CUDA events on the
-handle's stream, each step started with a cold L2 (a 256 MiB buffer is
-written before each timed step, outside the events); `e2e` repeats the
-steps through the public API with positions and velocities uploaded from and
-read back to pinned host memory every step.  Under torchrun every rank runs
-an independent replica (the scene does not shard) and rank 0 prints one
-JSON line with the whole-job throughput.
+handle's stream, an event before each stage, each step started with a cold
+L2 (a 256 MiB buffer is written before each timed step, outside the events),
+so the per-stage times and the roofline come from the same steps as the
+headline; the state 800 steps in (the crowded phase of the workload) is
+timed the same way and reported beside it.  `e2e` repeats the steps through
+the public API with positions and velocities uploaded from and read back to
+pinned host memory every step.  Under torchrun every rank runs an
+independent replica (the scene does not shard) and rank 0 prints one JSON
+line with the whole-job throughput.
 
 `--impl reference` times the CPU restatement of the reference's step (the
-oracle; the reference itself has no CPU path and its GPU code needs the
-reference tree) on all host cores, on a 131,072-particle sample of the same
-workload (two 64 x 16 x 64 columns, same spacing and constants).
+oracle; the reference itself has no CPU path) on all host cores, on the same
+1,048,576-particle workload with the same warm-up and step counts, with the
+SimParams the reference's own scene loader derived for it (recorded in
+tests/golden/scenes.npz); where the reference's kernels were compiled to PTX
+(oracle/_ref), their GPU step on the same workload is timed beside it
+(`reference_gpu`).  Nothing of the product library is loaded on that arm.
 """
 from __future__ import annotations
 

@@ -192,15 +192,23 @@ int sph_set_persistent(SphSystem* sys, int on);
    and the handle stays usable.  Needs persistent stepping on. */
 int sph_persistent_withheld(SphSystem* sys, uint32_t* flags);
 
-/* Launch shape of the density and force walks: 0 = 64 threads per block,
-   1 = 128 (default), 2 = 256, each compiled for full occupancy at that size. */
+/* Launch shape of the density and force walks.  0, 1, 2: one particle per
+   thread over global memory, 64, 128 or 256 threads per block, each compiled
+   for full occupancy at that size.  3, 4, 5: the candidates of the block's
+   neighbour cells staged in shared memory (room for 2048 / 1536, 4096 /
+   2560 and 1024 / 768 density / force candidates per block of 128, 256 and
+   128 threads; a block whose cells need more walks global memory).  1 is the
+   default.  Without neighbour masks (maxParInCell > 16) every shape walks
+   global memory.  Every shape gives the same bits. */
+#define SPH_WALK_SHAPES 6
 int sph_set_walk_shape(SphSystem* sys, uint32_t shape);
 int sph_get_walk_shape(SphSystem* sys, uint32_t* shape, uint32_t* threads_per_block);
 
 /* Autotuner: times `trial_steps` steps with each walk shape on this
    handle's own scenes and keeps the fastest (written to *chosen; per-shape
-   ms per step to ms_per_step[3] if not NULL).  The particle state is saved
-   before and restored after, so tuning does not advance the simulation. */
+   ms per step to ms_per_step[SPH_WALK_SHAPES] if not NULL).  The particle
+   state is saved before and restored after, so tuning does not advance the
+   simulation. */
 int sph_autotune(SphSystem* sys, uint32_t trial_steps, float* ms_per_step, uint32_t* chosen);
 
 /* One step with a CUDA event recorded on the handle's stream before the

@@ -29,8 +29,10 @@
 //   k_force            27-cell spiky + viscosity, collider, accelerators;
 //                      the new velocity is written in sorted order
 // so the sorted order (hash, original index) equals the reference's.
+#include <climits>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_bf16.h>
@@ -180,28 +182,49 @@ k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
              vel_start, i);
 }
 
-// Launch shapes of the two walks: (threads per block, minimum resident
-// blocks per SM) pairs (64, 16), (128, 8), (256, 4), i.e. 64 registers per
-// thread (the featured force pass: 7/8 of those blocks, 72 registers);
+// Launch shapes of the two walks.  Shapes 0-2 walk global memory, one
+// particle per thread: (threads per block, minimum resident blocks per SM)
+// pairs (64, 16), (128, 8), (256, 4), i.e. 64 registers per thread (the
+// featured force pass: 7/8 of those blocks, 72 registers).  Shapes 3-5 stage
+// the candidates in shared memory (sph_walk_tile.cuh) with 128 or 256
+// threads and room for kTileDensSlots / kTileForceSlots candidates per CTA.
 // sph_autotune picks one per handle by timing them on the handle's own
-// scenes.  Shape 1 (128 threads) is the default, the fastest on GB300 for
-// the 1M-particle dam break.
-constexpr int kWalkShapes = 3;
-constexpr int kWalkBlocks[kWalkShapes] = {64, 128, 256};
+// scenes; without neighbour masks (maxParInCell > 16) every shape walks
+// global memory.
+constexpr int kWalkShapes = 6;
+constexpr int kWalkBlocks[kWalkShapes] = {64, 128, 256, 128, 256, 128};
+constexpr bool kWalkTiled[kWalkShapes] = {false, false, false, true, true, true};
+constexpr uint32_t kTileDensSlots[kWalkShapes] = {0, 0, 0, 2048, 4096, 1024};
+constexpr uint32_t kTileForceSlots[kWalkShapes] = {0, 0, 0, 1536, 2560, 768};
 constexpr int kDefaultShape = 1;
+static_assert(kWalkShapes == SPH_WALK_SHAPES, "walk shapes in pibiti_sph.h");
 
-// Neighbour masks: with 3 * maxParInCell <= 64, the density pass records for
+// Neighbour masks: with maxParInCell <= 16, the density pass records for
 // each particle and each of the 9 neighbour rows (dz, dy) one 64-bit mask
-// over the row's candidates (the row's up to 3 cells, each truncated at
-// maxParInCell, concatenated in walk order): bit set = squared distance below
-// ForceConsts::h2_out (or NaN).  The force pass visits exactly those
-// candidates, in the same order, so its sums are unchanged, and skips the
-// rest, which the density pass has shown contribute nothing.
+// over the row's candidates: a 16-bit field per x offset (dx = -1 in bits
+// 32-47, dx = 0 in bits 16-31, dx = +1 in bits 0-15), and in a field, bit
+// 15 - k for the cell's k-th candidate (its k-th particle, k < maxParInCell).
+// Bit set = squared distance below ForceConsts::h2_out (or NaN).  The highest
+// set bit is the first candidate in walk order, so the force pass visits
+// exactly those candidates, in the same order, by repeatedly taking the
+// highest set bit; its sums are unchanged, and it skips the rest, which the
+// density pass has shown contribute nothing.  The layout does not depend on
+// how many particles the cells hold, so a walk that stages the candidates
+// somewhere else reads the same masks.
 constexpr int kRows = 9;
-constexpr uint32_t kMaskMaxPerCell = 21;
+constexpr uint32_t kMaskMaxPerCell = 16;
+constexpr int kMaskField = 16;
 #ifndef SPH_WALK_MASKS
 #define SPH_WALK_MASKS 1  // 0: no mask buffer (saves 72 B per particle)
 #endif
+
+// Field (dx + 1) and candidate index of mask bit b.
+__device__ __forceinline__ int mask_field(int b) { return 2 - (b >> 4); }
+__device__ __forceinline__ uint32_t mask_cand(int b) { return (uint32_t)(15 - (b & 15)); }
+// The field of a cell whose candidate k is bit k of `m` (k < 16).
+__device__ __forceinline__ unsigned long long mask_place(uint32_t m, int field) {
+  return (unsigned long long)(__brev(m) >> 16) << (16 * (2 - field));
+}
 
 __device__ __forceinline__ float h2_out_of(const SimParams& p) {
   return __int_as_float(__float_as_int(__fmul_rn(p.h, p.h)) + 2);
@@ -235,7 +258,6 @@ __device__ __forceinline__ void density_item(const SceneDesc* __restrict__ sc,
     unsigned long long rowmask = 0;
     if (z >= 0 && z < gz && y >= 0 && y < gy) {
       const uint32_t row = d.c_off + (uint32_t)(z * (int)p.gridSize_yx + y * gx);
-      uint32_t bit = 0;
 #pragma unroll 1
       for (int x = x0; x <= x1; ++x) {
         const uint32_t c = row + (uint32_t)x;
@@ -269,8 +291,7 @@ __device__ __forceinline__ void density_item(const SceneDesc* __restrict__ sc,
           for (uint32_t k = 0; k < n; ++k) cand(k);
         }
         sum = __fadd_rn(sum, cell);
-        if (kMask) rowmask |= (unsigned long long)m << bit;
-        bit += n;
+        if (kMask) rowmask |= mask_place(m, x - cx + 1);
       }
     }
     if (kMask) masks[(size_t)r * N + i] = rowmask;
@@ -399,28 +420,24 @@ __device__ __forceinline__ void force_item(const SceneDesc* __restrict__ sc,
       if (z < 0 || z >= gz || y < 0 || y >= gy) continue;
       unsigned long long m = masks[(size_t)r * N + i];
       if (!m) continue;
-      const uint32_t row = d.c_off + (uint32_t)(z * (int)p.gridSize_yx + y * gx) + (uint32_t)x0;
-      const int nc = x1 - x0 + 1;
-      const uint32_t n0 = min(ld<kNC>(count + row), maxpc);
-      const uint32_t n1 = nc > 1 ? min(ld<kNC>(count + row + 1), maxpc) : 0u;
-      const uint32_t s0 = ld<kNC>(start + row);
-      const uint32_t s1 = nc > 1 ? ld<kNC>(start + row + 1) : 0u;
-      const uint32_t s2 = nc > 2 ? ld<kNC>(start + row + 2) : 0u;
-      const uint32_t b1 = n0, b2 = n0 + n1;
+      // cell starts by field (dx + 1); a field outside the grid holds no bit
+      const uint32_t row = d.c_off + (uint32_t)(z * (int)p.gridSize_yx + y * gx) + (uint32_t)cx;
+      const uint32_t s0 = cx > 0 ? ld<kNC>(start + row - 1) : 0u;
+      const uint32_t s1 = ld<kNC>(start + row);
+      const uint32_t s2 = cx + 1 < gx ? ld<kNC>(start + row + 1) : 0u;
       int cur = -1;
-      auto cell_of_bit = [&](uint32_t b) { return b >= b2 ? 2 : (b >= b1 ? 1 : 0); };
-      auto index_of_bit = [&](uint32_t b, int c) {
-        return c == 0 ? s0 + b : (c == 1 ? s1 + (b - b1) : s2 + (b - b2));
+      auto index_of_bit = [&](int b, int c) {
+        return (c == 0 ? s0 : (c == 1 ? s1 : s2)) + mask_cand(b);
       };
       // Two set bits per iteration: the two terms are independent (their
       // loads, square roots and divisions overlap) and are added in order.
       while (m) {
-        const uint32_t ba = (uint32_t)(__ffsll((long long)m) - 1);
-        m &= m - 1;
+        const int ba = 63 - __clzll((long long)m);
+        m ^= 1ull << ba;
         const bool two = m != 0;
-        const uint32_t bb = two ? (uint32_t)(__ffsll((long long)m) - 1) : ba;
-        m &= two ? m - 1 : m;
-        const int ca = cell_of_bit(ba), cb = cell_of_bit(bb);
+        const int bb = two ? 63 - __clzll((long long)m) : ba;
+        if (two) m ^= 1ull << bb;
+        const int ca = mask_field(ba), cb = mask_field(bb);
         float3 fa_, fb_;
         const bool ina = term(index_of_bit(ba, ca), fa_, true);
         const bool inb = term(index_of_bit(bb, cb), fb_, two);
@@ -576,6 +593,8 @@ k_force(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
   if (i >= N) return;
   force_item<kMask, kFeat>(sc, poff, S, N, pos, vel, dens, dp, start, count, masks, vel_out, fo, i);
 }
+
+#include "sph_walk_tile.cuh"
 
 // After a coarse step of dt_c = n dt (sorted order).  Within a step,
 // gravity and the wall kicks act before the drift (integrate) and the SPH
@@ -1187,13 +1206,65 @@ void launch_walks_shape(SphSystem* s, cudaStream_t st, int b, int v, const StepO
         s->count, s->masks, s->vel[v], o.fo);
 }
 
+inline size_t tile_smem_density(uint32_t slots) { return sizeof(TileTables) + 3 * sizeof(float) * slots; }
+inline size_t tile_smem_force(uint32_t slots) { return sizeof(TileTables) + 2 * sizeof(float4) * slots; }
+
+// Staged walks (shapes 3-5).  The featured force pass of the learned step
+// keeps the global-memory walk.
+template <int kThreads, class Mark>
+void launch_walks_tile(SphSystem* s, cudaStream_t st, int b, int v, const StepOpts& o, Mark& mark,
+                       uint32_t dslots, uint32_t fslots) {
+  const unsigned g = grid_for(s->N, kThreads);
+  k_density_tile<kThreads><<<g, kThreads, tile_smem_density(dslots), st>>>(
+      o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->start, s->count, s->dens, s->pres, s->dp, s->masks,
+      s->flags, dslots);
+  mark();
+  if (o.feat)
+    k_force<true, 128, 8, true><<<grid_for(s->N, 128), 128, 0, st>>>(
+        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->dp, s->start, s->count,
+        s->masks, s->vel[v], o.fo);
+  else
+    k_force_tile<kThreads><<<g, kThreads, tile_smem_force(fslots), st>>>(
+        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->dp, s->start, s->count,
+        s->masks, s->vel[v], fslots);
+}
+
 template <bool kMask, class Mark>
 void launch_walks(SphSystem* s, cudaStream_t st, int b, int v, const StepOpts& o, Mark& mark) {
-  switch (s->walk_shape) {
-    case 0: launch_walks_shape<kMask, 64, 16>(s, st, b, v, o, mark); break;
-    case 2: launch_walks_shape<kMask, 256, 4>(s, st, b, v, o, mark); break;
+  const int shape = s->walk_shape;
+  if (kMask && kWalkTiled[shape]) {
+    if (kWalkBlocks[shape] == 256)
+      launch_walks_tile<256>(s, st, b, v, o, mark, kTileDensSlots[shape], kTileForceSlots[shape]);
+    else
+      launch_walks_tile<128>(s, st, b, v, o, mark, kTileDensSlots[shape], kTileForceSlots[shape]);
+    return;
+  }
+  switch (kWalkBlocks[shape]) {
+    case 64: launch_walks_shape<kMask, 64, 16>(s, st, b, v, o, mark); break;
+    case 256: launch_walks_shape<kMask, 256, 4>(s, st, b, v, o, mark); break;
     default: launch_walks_shape<kMask, 128, 8>(s, st, b, v, o, mark); break;
   }
+}
+
+// Shared memory the staged walks may use (set once per handle).
+int tile_attributes() {
+  size_t dmax128 = 0, fmax128 = 0, dmax256 = 0, fmax256 = 0;
+  for (int k = 0; k < kWalkShapes; ++k) {
+    if (!kWalkTiled[k]) continue;
+    size_t& dm = kWalkBlocks[k] == 256 ? dmax256 : dmax128;
+    size_t& fm = kWalkBlocks[k] == 256 ? fmax256 : fmax128;
+    dm = std::max(dm, tile_smem_density(kTileDensSlots[k]));
+    fm = std::max(fm, tile_smem_force(kTileForceSlots[k]));
+  }
+  SPH_CUDA(cudaFuncSetAttribute(k_density_tile<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dmax128),
+           "staged density walk shared memory");
+  SPH_CUDA(cudaFuncSetAttribute(k_density_tile<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dmax256),
+           "staged density walk shared memory");
+  SPH_CUDA(cudaFuncSetAttribute(k_force_tile<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fmax128),
+           "staged force walk shared memory");
+  SPH_CUDA(cudaFuncSetAttribute(k_force_tile<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fmax256),
+           "staged force walk shared memory");
+  return SPH_OK;
 }
 
 // Enqueues one step on `st`, advancing s->cp.  With `ev` (kStepStages + 1
@@ -1345,6 +1416,7 @@ int create(const SimParams* scenes, uint32_t count, SphSystem** out) {
     rc = cuda_check(cudaFuncSetAttribute(k_sort_big_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(kBlockSortMax * sizeof(uint32_t))),
                     "crowded-cell sort shared memory");
+  if (rc == SPH_OK) rc = tile_attributes();
   if (rc == SPH_OK) {
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);

@@ -291,7 +291,8 @@ class SPH:
         """update(k) as one cooperative launch of k steps (same results)."""
         check(lib().sph_set_persistent(self._h, int(on)))
 
-    WALK_THREADS = (64, 128, 256)
+    WALK_THREADS = (64, 128, 256, 128, 256, 128)  # by shape (sph_set_walk_shape)
+    WALK_STAGED = (False, False, False, True, True, True)
 
     def set_walk_shape(self, shape: int) -> None:
         check(lib().sph_set_walk_shape(self._h, shape))
@@ -304,7 +305,7 @@ class SPH:
     def autotune(self, trial_steps: int = 10):
         """Pick the fastest walk launch shape on this handle's scenes; returns
         (chosen shape, ms per step of each shape).  State is unchanged."""
-        ms = (ctypes.c_float * 3)()
+        ms = (ctypes.c_float * len(self.WALK_THREADS))()
         ch = ctypes.c_uint32()
         check(lib().sph_autotune(self._h, trial_steps, ms, ctypes.byref(ch)))
         return ch.value, list(ms)
