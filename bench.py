@@ -122,21 +122,70 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_summary(key: str, kernel: str):
-    """A per-launch figure of `kernel` from the committed ncu summary of this
-    workload (profiles/): `traffic` (DRAM bytes read + written) or `issue`
+CROWDED_STEP = 800      # the crowded phase, timed beside the headline steps
+ENSEMBLE_STEPS = 500    # steps of the ensemble measurement (one CUDA graph)
+WALK_PROFILE = os.path.join("profiles", "walk_kernels_double_dambreak_1M.md")
+SMS = 152               # GB300 multiprocessors
+ISSUE_PER_SM_CLOCK = 4  # warp instructions issued per SM per clock (4 schedulers)
+
+
+def ncu_summary(key: str, kernel: str, state: str):
+    """A per-launch figure of `kernel` at `state` ("early", "crowded") from
+    the committed ncu summary of this workload: `traffic` (DRAM bytes read +
+    written), `instructions` (warp instructions executed) or `issue`
     (fraction of issue slots busy); None if it has no entry."""
-    path = os.path.join(ROOT, "profiles", "walk_kernels_double_dambreak_1M.md")
+    path = os.path.join(ROOT, WALK_PROFILE)
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.startswith(f"{key} {kernel}:"):
+        if line.startswith(f"{key} {kernel} {state}:"):
             return float(line.split(":")[1].split()[0])
     return None
 
 
-def ncu_traffic(kernel: str):
-    return ncu_summary("traffic", kernel)
+def timed_steps(sysm, stream, flush, steps: int):
+    """`steps` steps, each after a write of `flush` (larger than L2) and with
+    a CUDA event before each stage on the handle's stream: per-step ms and
+    per-stage lists of ms."""
+    import torch
+    from pibiti_gb300.sph import SPH
+    step_ms, stages = [], {k: [] for k in SPH.STAGES}
+    with torch.cuda.stream(stream):
+        for k in range(steps):
+            flush.fill_(k & 0xff)
+            st = sysm.step_timed()
+            for name, v in st.items():
+                stages[name].append(v)
+            step_ms.append(sum(st.values()))
+    return step_ms, stages
+
+
+def stage_roofline(stages: dict, n: int, cells: int, peak: float, peak_kind: str, walk: dict,
+                   state: str, sm_mhz, where: str) -> dict:
+    """HBM roofline of the dominant stage (median over the given steps):
+    its algorithmic bytes per launch over its CUDA-event time, against the
+    measured copy bandwidth; beside it the issue-slot roof of the same
+    kernel: its warp instructions per launch (the committed ncu summary of
+    the same state) over SMS x 4 issue slots per clock at the sampled SM
+    clock."""
+    stage_ms = {k: statistics.median(v) for k, v in stages.items()}
+    dom = max(stage_ms, key=stage_ms.get)
+    bp, bc = STAGE_BYTES[dom]
+    alg = bp * n + bc * cells
+    achieved = alg / (stage_ms[dom] / 1e3) / 1e9
+    kernel = f"k_{dom}" + ("_tile" if walk.get("staged") and dom in ("density", "force") else "")
+    traffic = ncu_summary("traffic", kernel, state)
+    instr = ncu_summary("instructions", kernel, state)
+    binding = None
+    if instr and sm_mhz:
+        issue_ms = instr / (SMS * ISSUE_PER_SM_CLOCK * sm_mhz * 1e3)
+        binding = {"resource": "instruction issue", "warp_instructions": instr,
+                   "issue_roof_ms": issue_ms, "frac": issue_ms / stage_ms[dom],
+                   "sm_mhz": sm_mhz, "source": f"{WALK_PROFILE} ({state} state)"}
+    return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "traffic_state": state,
+            "algorithmic_bytes": alg, "peak_source": peak_kind, "stage_ms": stage_ms,
+            "stage_ms_sum": sum(stage_ms.values()), "steps": where, "binding": binding}
 
 
 class ClockSampler:
@@ -189,26 +238,62 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_sample_workload():
-    from pibiti_gb300 import configs
-    return configs.dambreak_double(ny=16)
+def reference_params(xml: str) -> bytes:
+    """SimParams bytes the reference's own scene loader (Scene.cpp,
+    Scene_Load.cpp, run through oracle/ref_emu) derived for the scene element
+    `xml`, as recorded in tests/golden/scenes.npz by
+    tests/golden/make_golden.py.  The reference arm takes its parameters
+    from here, not from the product's loader."""
+    with np.load(os.path.join(ROOT, "tests", "golden", "scenes.npz")) as z:
+        xmls = [str(x) for x in z["xml"]]
+        if xml not in xmls:
+            raise KeyError("workload scene element not in tests/golden/scenes.npz "
+                           "(regenerate it with tests/golden/make_golden.py)")
+        return z["params"][xmls.index(xml)].tobytes()
 
 
-def time_cpu_oracle(budget_s: float, min_steps: int = 3):
-    """Oracle (single-precision restatement) steps on the 131,072-particle
-    sample until `budget_s` of CPU work; returns (particle-steps/s, steps, threads)."""
+def time_cpu_oracle(params: bytes, pos, vel, warmup: int, steps: int):
+    """The oracle's single-precision step (OpenMP, all host threads) on the
+    full workload: `warmup` untimed steps, then `steps` timed steps in one
+    call.  Returns (particle-steps/s, seconds, threads)."""
     import oracle
-    from pibiti_gb300.sph import Scene
-    w = cpu_sample_workload()
-    p = Scene.parse(w.xml).params
-    pos, vel = oracle.step(p, w.pos, w.vel, steps=1)  # warm-up (allocations, page-in)
-    steps, t = 0, 0.0
-    while steps < min_steps or t < budget_s:
-        t0 = time.perf_counter()
-        pos, vel = oracle.step(p, pos, vel, steps=1)
-        t += time.perf_counter() - t0
-        steps += 1
-    return w.n * steps / t, steps, oracle.threads(), w.n
+    if warmup:
+        pos, vel = oracle.step(params, pos, vel, steps=warmup)
+    t0 = time.perf_counter()
+    oracle.step(params, pos, vel, steps=steps)
+    dt = time.perf_counter() - t0
+    return len(pos) * steps / dt, dt, oracle.threads()
+
+
+def time_reference_gpu(params: bytes, pos, vel, warmup: int, steps: int):
+    """The reference's own CUDA kernels (System.cu, radixsort_kernel.cu,
+    compiled to PTX with nvcc's default flags by oracle/ref_gpu/build_ref_gpu.sh)
+    stepping the same workload on this GPU as cSPH::Update does, every
+    wrapper ending with a device synchronisation (SPH_Update.cpp:39-76,
+    System.cu:653-756): wall time of `steps` steps after `warmup`.  None
+    where the PTX or the GPU is missing."""
+    try:
+        import torch
+        import oracle.ref_gpu as rg
+        if not torch.cuda.is_available() or not rg.available():
+            return None
+    except Exception:  # no harness on this machine
+        return None
+    from pibiti_gb300.params import SimParams  # the ABI struct's layout only (ctypes)
+    p = SimParams.from_bytes(params)
+    r = rg.RefStep(p, pos, vel, fast=True)
+    r.update(warmup)
+    torch.cuda.synchronize()
+    stage = {}
+    t0 = time.perf_counter()
+    r.update(steps, stage)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return {"value": len(pos) * steps / dt, "unit": UNIT, "ms_per_step": 1e3 * dt / steps,
+            "stage_ms": {k: 1e3 * v / steps for k, v in stage.items()},
+            "note": "the reference's own kernels on this GPU, launched with its wrappers' grids "
+                    "and a device synchronisation after each wrapper; same workload, warm-up "
+                    "and step count as this line"}
 
 
 def run_cpu_configs(args) -> int:
@@ -237,23 +322,19 @@ def run_cpu_configs(args) -> int:
 
 
 def run_reference(args):
+    """The reference arm: the oracle's CPU step on the full workload (the
+    reference has no CPU path of its own), rank 0 only; the reference's own
+    GPU kernels on the same workload beside it where they are built."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    import oracle
-    from pibiti_gb300.sph import Scene
-    w = cpu_sample_workload()
-    p = Scene.parse(w.xml).params
-    pos, vel = w.pos, w.vel
-    for _ in range(args.warmup):
-        pos, vel = oracle.step(p, pos, vel, steps=1)
-    t0 = time.perf_counter()
-    pos, vel = oracle.step(p, pos, vel, steps=args.steps)
-    dt = time.perf_counter() - t0
-    value = w.n * args.steps / dt
-    threads = oracle.threads()
-    sample = (f"{w.n} particles (two 64x16x64 columns of the double dam break, same spacing, "
-              f"h and constants), {args.steps} full steps")
+    from pibiti_gb300 import configs
+    w = configs.dambreak_double()
+    params = reference_params(w.xml)
+    value, dt, threads = time_cpu_oracle(params, w.pos, w.vel, args.warmup, args.steps)
+    sample = (f"the full workload ({w.n} particles), {args.warmup} untimed then {args.steps} "
+              f"timed steps, oracle single-precision restatement, SimParams from the "
+              f"reference's scene loader")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
@@ -262,44 +343,136 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_gpu": time_reference_gpu(params, w.pos, w.vel, args.warmup, args.steps),
         "notes": "The reference has no CPU implementation of its step; this is the oracle's "
                  "single-precision restatement of it (oracle/sph_oracle.c), OpenMP on all "
-                 "host threads.",
+                 "host threads, on the same workload as our arm.",
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
+def ensemble_single(e, ps, stream, warmup: int, steps: int) -> dict:
+    """The ensemble `e` (scene parameters `ps`) in one handle on this GPU:
+    `warmup` steps, the autotuner, then `steps` steps captured as one CUDA
+    graph and launched once (CUDA events); beside it the same steps as one
+    persistent cooperative launch, and the first 32 scenes stepped one
+    handle each."""
+    import torch
+    from pibiti_gb300.sph import ARRAY_POS, ARRAY_VEL, SPH
+    sysm = SPH(ps, stream=stream)
+    sysm.set_array(ARRAY_POS, e.pos)
+    sysm.set_array(ARRAY_VEL, e.vel)
+    sysm.update(warmup)
+    chosen, tune_ms = sysm.autotune(trial_steps=5)
+    sysm.set_graph_steps(steps)
+    sysm.update(steps)  # builds and runs the graph once (untimed)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sysm.update(steps)  # one graph launch
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    st = sysm.stats()
+    sysm.close()
+    # the same steps as one persistent cooperative launch, from the same start
+    with SPH(ps, stream=stream) as ph:
+        ph.set_array(ARRAY_POS, e.pos)
+        ph.set_array(ARRAY_VEL, e.vel)
+        ph.set_persistent(True)
+        ph.update(warmup)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        ph.update(steps)  # one launch
+        p1.record(stream)
+        torch.cuda.synchronize()
+        pms = p0.elapsed_time(p1)
+        persistent = {"value": ph.n * steps / (pms / 1e3), "unit": UNIT, "ms_per_step": pms / steps,
+                      "barrier_timeout": bool(ph.flags() & 4),
+                      "note": f"{steps} steps in one cooperative launch (grid barrier between stages)"}
+    # the same scenes, one handle each, for the first 32 scenes
+    sub = 32
+    t_sep, n_sep = 0.0, 0
+    off = 0
+    for k in range(sub):
+        nk = e.sizes[k]
+        with SPH(ps[k], stream=stream) as one:
+            one.set_array(ARRAY_POS, e.pos[off:off + nk])
+            one.set_array(ARRAY_VEL, e.vel[off:off + nk])
+            one.update(4)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            one.update(50)
+            b.record(stream)
+            torch.cuda.synchronize()
+            t_sep += a.elapsed_time(b) / 1e3
+            n_sep += nk * 50
+        off += nk
+    return {
+        "metric": "ensemble particle-steps/s", "value": e.n * steps / (ms / 1e3), "unit": UNIT,
+        "steps": steps, "warmup": warmup, "ms_per_step": ms / steps,
+        "config": {"workload": f"batched ensemble: {len(ps)} dam-break scenes, "
+                               f"{min(e.sizes)}-{max(e.sizes)} particles (log-uniform, x512), "
+                               f"k in [1,5], mu in [1,6]", "particles": e.n,
+                   "cells": int(sum(p.numCells for p in ps)),
+                   "graph": f"{steps} steps captured as one CUDA graph, one launch"},
+        "autotune": {"chosen_shape": chosen, "chosen_threads": SPH.WALK_THREADS[chosen],
+                     "staged": SPH.WALK_STAGED[chosen], "ms_per_step": tune_ms},
+        "separate_handles": {"scenes": sub, "value": n_sep / t_sep, "unit": UNIT},
+        "persistent": persistent,
+        "state_check": {"max_density_dev": float(st[:, 2].max()), "nonfinite": float(st[:, 3].sum())},
+    }
+
+
+def measure_ensemble(warmup: int, steps: int) -> dict:
+    """The 256-scene ensemble on this GPU (ensemble_single)."""
+    import torch
+    from pibiti_gb300 import configs
+    from pibiti_gb300.sph import Scene
+    e = configs.ensemble(steps=steps)
+    ps = [Scene.parse(x).params for x in e.xmls]
+    return ensemble_single(e, ps, torch.cuda.Stream(), warmup, steps + (steps % 2))
+
+
 def run_ensemble(args):
     """256 independent dam-break scenes (4k-64k particles, k in [1,5], mu in
-    [1,6]) stepped together in one handle: `steps` steps captured as one CUDA
-    graph and launched once, after the autotuner picked the walk shape.  The
-    same scenes stepped one handle at a time (first 32 scenes) are timed for
-    comparison."""
+    [1,6]) stepped together in one handle per GPU: `steps` steps captured as
+    one CUDA graph and launched once, after the autotuner picked the walk
+    shape.  Under torchrun the scenes are split over the ranks with no
+    exchange."""
     import torch
     from pibiti_gb300 import configs
     from pibiti_gb300.sph import ARRAY_POS, ARRAY_VEL, SPH, Scene
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    steps = args.steps + (args.steps % 2)
+    if world == 1:
+        clocks = ClockSampler(local)
+        clocks.start()
+        line = measure_ensemble(args.warmup, steps)
+        line.update({"n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+                     "clocks": clocks.stop()})
+        print(json.dumps(line), flush=True)
+        return 0
+    import torch.distributed as dist
+    dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     e = configs.ensemble(steps=args.steps)
     total = e.n
-    if world > 1:  # independent scenes: each rank steps its share, no exchange
-        mine = shard_scenes(e.sizes, world, rank)
-        offs = np.concatenate([[0], np.cumsum(e.sizes)])
-        sel = np.concatenate([np.arange(offs[k], offs[k + 1]) for k in mine])
-        e = configs.Ensemble(e.name, [e.xmls[k] for k in mine], e.pos[sel], e.vel[sel],
-                             [e.sizes[k] for k in mine], e.steps, dict(e.notes, scenes=mine))
+    mine = shard_scenes(e.sizes, world, rank)  # independent scenes: no exchange
+    offs = np.concatenate([[0], np.cumsum(e.sizes)])
+    sel = np.concatenate([np.arange(offs[k], offs[k + 1]) for k in mine])
+    e = configs.Ensemble(e.name, [e.xmls[k] for k in mine], e.pos[sel], e.vel[sel],
+                         [e.sizes[k] for k in mine], e.steps, dict(e.notes, scenes=mine))
     ps = [Scene.parse(x).params for x in e.xmls]
     stream = torch.cuda.Stream()
     sysm = SPH(ps, stream=stream)
     sysm.set_array(ARRAY_POS, e.pos)
     sysm.set_array(ARRAY_VEL, e.vel)
     sysm.update(args.warmup)
-    chosen, tune_ms = sysm.autotune(trial_steps=5)
-    steps = args.steps + (args.steps % 2)
+    sysm.autotune(trial_steps=5)
     sysm.set_graph_steps(steps)
     sysm.update(steps)  # builds and runs the graph once (untimed)
     torch.cuda.synchronize()
@@ -316,71 +489,17 @@ def run_ensemble(args):
     clk = clocks.stop()
     ms = max_over_ranks(e0.elapsed_time(e1), device="cuda")
     value = ensemble_throughput(total, steps, ms)
-    st = sysm.stats()
     sysm.close()
-    if world > 1:  # the single-GPU comparisons below are not repeated per rank
-        if rank == 0:
-            print(json.dumps({
-                "metric": "ensemble particle-steps/s", "value": value, "unit": UNIT, "n_gpus": world,
-                "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps,
-                "higher_is_better": True, "scaling": "strong", "dtype": "f32", "data": "synthetic",
-                "config": {"workload": "batched ensemble: 256 dam-break scenes split over the GPUs by "
-                                       "particle count (no exchange)", "particles": total,
-                           "graph": f"{steps} steps captured as one CUDA graph per rank"},
-                "clocks": clk}), flush=True)
-        torch.distributed.destroy_process_group()
-        return 0
-    # the same steps as one persistent cooperative launch, from the same start
-    with SPH(ps, stream=stream) as ph:
-        ph.set_array(ARRAY_POS, e.pos)
-        ph.set_array(ARRAY_VEL, e.vel)
-        ph.set_persistent(True)
-        ph.update(args.warmup)
-        torch.cuda.synchronize()
-        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        p0.record(stream)
-        ph.update(steps)  # one launch
-        p1.record(stream)
-        torch.cuda.synchronize()
-        pms = p0.elapsed_time(p1)
-        persistent = {"value": ph.n * steps / (pms / 1e3), "unit": UNIT, "ms_per_step": pms / steps,
-                      "barrier_timeout": bool(ph.flags() & 4),
-                      "note": f"{steps} steps in one cooperative launch (grid barrier between stages)"}
-    # the same scenes, one handle each, for the first 32 scenes
-    sub = 32
-    t_sep, n_sep = 0.0, 0
-    off = 0
-    for k in range(sub):
-        n = e.sizes[k]
-        with SPH(ps[k], stream=stream) as one:
-            one.set_array(ARRAY_POS, e.pos[off:off + n])
-            one.set_array(ARRAY_VEL, e.vel[off:off + n])
-            one.update(4)
-            torch.cuda.synchronize()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            one.update(50)
-            b.record(stream)
-            torch.cuda.synchronize()
-            t_sep += a.elapsed_time(b) / 1e3
-            n_sep += n * 50
-        off += n
-    line = {
-        "metric": "ensemble particle-steps/s", "value": value, "unit": UNIT,
-        "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps,
-        "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"batched ensemble: {len(ps)} dam-break scenes, "
-                               f"{min(e.sizes)}-{max(e.sizes)} particles (log-uniform, x512), "
-                               f"k in [1,5], mu in [1,6]", "particles": e.n,
-                   "cells": int(sum(p.numCells for p in ps)),
-                   "graph": f"{steps} steps captured as one CUDA graph, one launch"},
-        "autotune": {"chosen_threads": SPH.WALK_THREADS[chosen], "ms_per_step": tune_ms},
-        "separate_handles": {"scenes": sub, "value": n_sep / t_sep, "unit": UNIT},
-        "persistent": persistent,
-        "clocks": clk,
-        "state_check": {"max_density_dev": float(st[:, 2].max()), "nonfinite": float(st[:, 3].sum())},
-    }
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "ensemble particle-steps/s", "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": ms / steps,
+            "higher_is_better": True, "scaling": "strong", "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batched ensemble: 256 dam-break scenes split over the GPUs by "
+                                   "particle count (no exchange)", "particles": total,
+                       "graph": f"{steps} steps captured as one CUDA graph per rank"},
+            "clocks": clk}), flush=True)
+    dist.destroy_process_group()
     return 0
 
 
@@ -551,6 +670,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-form measurement")
     ap.add_argument("--no-render", action="store_true", help="skip the render measurement")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble measurement")
     ap.add_argument("--save-state", metavar="NPZ",
                     help="profiling aid: run --warm-steps steps of the workload, save the state, exit")
     ap.add_argument("--stages", metavar="NPZ",
@@ -568,7 +688,6 @@ def main():
     if args.workload == "ensemble":
         return run_ensemble(args)
 
-    import numpy as np
     import torch
 
     rank, world, local = dist_env()
@@ -580,50 +699,61 @@ def main():
     from pibiti_gb300 import configs
     from pibiti_gb300.sph import ARRAY_POS, ARRAY_VEL, SPH, Scene
 
-    # CPU baseline first (no GPU work has started; rank 0 at N=1 only)
+    w = configs.dambreak_double(seed=42 + rank)
+
+    # CPU baseline first (no GPU work has started; rank 0 at N=1 only): the
+    # oracle on the full workload for about --cpu-budget seconds
     cpu = None
     if rank == 0 and world == 1 and args.cpu_budget > 0:
-        v, steps, threads, n = time_cpu_oracle(args.cpu_budget)
+        params = reference_params(configs.dambreak_double().xml)
+        v1, t1, _ = time_cpu_oracle(params, w.pos, w.vel, 1, 1)
+        k = max(3, int(args.cpu_budget / max(t1, 1e-3)))
+        v, _, threads = time_cpu_oracle(params, w.pos, w.vel, 1, k)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{n} particles (two 64x16x64 columns of the same dam break), "
-                         f"{steps} full steps, oracle single-precision restatement"}
+               "sample": f"the full workload ({w.n} particles), steps 2-{k + 1}, oracle "
+                         f"single-precision restatement, OpenMP on all host threads"}
 
-    w = configs.dambreak_double(seed=42 + rank)
     p = Scene.parse(w.xml).params
     stream = torch.cuda.Stream()
     sysm = SPH(p, stream=stream)
     sysm.set_array(ARRAY_POS, w.pos)
     sysm.set_array(ARRAY_VEL, w.vel)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    walk = {"shape": sysm.walk_shape(), "threads": SPH.WALK_THREADS[sysm.walk_shape()],
+            "staged": SPH.WALK_STAGED[sysm.walk_shape()]}
 
     with torch.cuda.stream(stream):
         sysm.update(args.warmup)
     torch.cuda.synchronize()
+    stepped = args.warmup
 
     clocks = ClockSampler(local)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks.start()
     time.sleep(0.3)
     wall0 = time.perf_counter()
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            flush.fill_(k & 0xff)
-            starts[k].record(stream)
-            sysm.update(1)
-            ends[k].record(stream)
+    step_ms, stages = timed_steps(sysm, stream, flush, args.steps)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    stepped += args.steps
     total_ms = max_over_ranks(sum(step_ms), device="cuda")
     n = sysm.n
     value = job_throughput(n, args.steps, world, total_ms)
+    peak, peak_kind = measured_peaks()
+    state = "early" if stepped <= 400 else "crowded"
+    roofline = stage_roofline(stages, n, p.numCells, peak, peak_kind, walk, state,
+                              clk.get("sm_mhz"), f"steps {args.warmup}-{stepped} (the timed steps)")
+    P = 4 if p.numCells >= 65536 else 2
+    model_b = 256 + 24 * P + 12 * p.numCells / n
+    step_gbs = model_b * n / (total_ms / args.steps / 1e3) / 1e9
+    roofline_step = {"bytes_per_particle_step": model_b, "achieved": step_gbs, "peak": peak,
+                     "unit": "GB/s", "frac": step_gbs / peak,
+                     "note": "reference dataflow byte model B = 256 + 24P + 12C/N"}
 
     # warm multi-step throughput (graph replay, L2 not flushed): informative
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -633,34 +763,7 @@ def main():
     e1.record(stream)
     torch.cuda.synchronize()
     warm_ms = e0.elapsed_time(e1) / warm_steps
-
-    # per-stage times (CUDA events on the handle's stream), cold L2
-    stages = {k: [] for k in SPH.STAGES}
-    for _ in range(20):
-        with torch.cuda.stream(stream):
-            flush.fill_(1)
-        for k, v in sysm.step_timed().items():
-            stages[k].append(v)
-    stage_ms = {k: statistics.median(v) for k, v in stages.items()}
-    dom = max(stage_ms, key=stage_ms.get)
-    bp, bc = STAGE_BYTES[dom]
-    alg = bp * n + bc * p.numCells
-    peak, peak_kind = measured_peaks()
-    achieved = alg / (stage_ms[dom] / 1e3) / 1e9
-    traffic = ncu_traffic(f"k_{dom}")
-    issue = ncu_summary("issue", f"k_{dom}")
-    roofline = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                "algorithmic_bytes": alg, "peak_source": peak_kind,
-                "stage_ms": stage_ms,
-                "binding": {"resource": "instruction issue", "issue_active_frac": issue,
-                            "source": "profiles/walk_kernels_double_dambreak_1M.md (ncu, crowded state)"}}
-    P = 4 if p.numCells >= 65536 else 2
-    model_b = 256 + 24 * P + 12 * p.numCells / n
-    step_gbs = model_b * n / (total_ms / args.steps / 1e3) / 1e9
-    roofline_step = {"bytes_per_particle_step": model_b, "achieved": step_gbs, "peak": peak,
-                     "unit": "GB/s", "frac": step_gbs / peak,
-                     "note": "reference dataflow byte model B = 256 + 24P + 12C/N"}
+    stepped += warm_steps
 
     # end to end through the public API with pinned host buffers
     hpos = torch.empty((n, 4), dtype=torch.float32).pin_memory()
@@ -680,11 +783,31 @@ def main():
     torch.cuda.synchronize()
     e2e_ms = max_over_ranks(es.elapsed_time(ee), device="cuda")
     e2e_value = job_throughput(n, args.e2e_steps, world, e2e_ms)
+    stepped += args.e2e_steps
+
+    # the crowded phase: the same handle stepped on to step CROWDED_STEP,
+    # then timed as the headline steps are
+    crowded = None
+    if rank == 0 and stepped < CROWDED_STEP:
+        sysm.update(CROWDED_STEP - stepped)
+        stepped = CROWDED_STEP
+        cms, cst = timed_steps(sysm, stream, flush, 10)
+        stepped += 10
+        crowded = {"steps": f"{CROWDED_STEP}-{stepped}", "ms_per_step": sum(cms) / len(cms),
+                   "value": n * len(cms) / (sum(cms) / 1e3), "unit": UNIT,
+                   "roofline": stage_roofline(cst, n, p.numCells, peak, peak_kind, walk, "crowded",
+                                              clk.get("sm_mhz"), f"steps {CROWDED_STEP}-{stepped}")}
 
     learned = measure_learned(w, p, stream) if rank == 0 and not args.no_learned else None
     render = measure_render(sysm, p, stream) if rank == 0 and not args.no_render else None
+    ensemble = None
+    if rank == 0 and world == 1 and not args.no_ensemble:
+        sysm_state = sysm.stats()[0]
+        ensemble = measure_ensemble(args.warmup, ENSEMBLE_STEPS)
+    else:
+        sysm_state = sysm.stats()[0]
 
-    st = sysm.stats()[0]
+    st = sysm_state
     flags = sysm.flags()
     if rank == 0:
         line = {
@@ -693,14 +816,17 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": workload_config(p),
             "parallelism": f"replicas x{world}" if world > 1 else "single",
+            "walk": walk,
             "e2e": {"value": e2e_value, "unit": UNIT, "steps": args.e2e_steps,
                     "h2d_bytes_per_step": 2 * n * 16, "d2h_bytes_per_step": 2 * n * 16},
             "roofline": roofline, "roofline_step": roofline_step,
+            "crowded": crowded,
             "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": KERNELS_PER_STEP * args.steps,
             "warm_ms_per_step": warm_ms,
             "wall_s_timed_loop": wall,
             "learned": learned,
+            "ensemble": ensemble,
             "render": render,
             "state_check": {"kinetic_energy": st[0], "mean_density": st[1],
                             "max_density_dev": st[2], "nonfinite": st[3], "flags": flags},
@@ -710,7 +836,6 @@ def main():
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
-
 
 if __name__ == "__main__":
     sys.exit(main())

@@ -192,15 +192,24 @@ int sph_set_persistent(SphSystem* sys, int on);
    and the handle stays usable.  Needs persistent stepping on. */
 int sph_persistent_withheld(SphSystem* sys, uint32_t* flags);
 
-/* Launch shape of the density and force walks.  0, 1, 2: one particle per
-   thread over global memory, 64, 128 or 256 threads per block, each compiled
-   for full occupancy at that size.  3, 4, 5: the candidates of the block's
-   neighbour cells staged in shared memory (room for 2048 / 1536, 4096 /
-   2560 and 1024 / 768 density / force candidates per block of 128, 256 and
-   128 threads; a block whose cells need more walks global memory).  1 is the
+/* Launch shape of the density and force walks: threads per block and the
+   form of each walk (every shape gives the same bits).
+     shape  threads  density                     force
+       0      64     global memory               global, row masks
+       1     128     global memory               global, row masks
+       2     256     global memory               global, row masks
+       3     128     staged in shared memory     staged in shared memory
+       4     128     staged, interleaved pairs   global, one cell at a time
+       5     256     staged, interleaved pairs   global, one cell at a time
+       6     128     staged, interleaved pairs   global, row masks
+       7     128     global memory               global, one cell at a time
+       8      64     staged, interleaved pairs   global, one cell at a time
+   "Staged": the candidates of the block's neighbour cells are copied to
+   shared memory once per block (a block whose cells need more room, or
+   whose particles belong to two scenes, walks global memory).  4 is the
    default.  Without neighbour masks (maxParInCell > 16) every shape walks
-   global memory.  Every shape gives the same bits. */
-#define SPH_WALK_SHAPES 6
+   global memory. */
+#define SPH_WALK_SHAPES 9
 int sph_set_walk_shape(SphSystem* sys, uint32_t shape);
 int sph_get_walk_shape(SphSystem* sys, uint32_t* shape, uint32_t* threads_per_block);
 

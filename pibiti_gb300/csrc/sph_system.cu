@@ -182,21 +182,27 @@ k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
              vel_start, i);
 }
 
-// Launch shapes of the two walks.  Shapes 0-2 walk global memory, one
-// particle per thread: (threads per block, minimum resident blocks per SM)
-// pairs (64, 16), (128, 8), (256, 4), i.e. 64 registers per thread (the
-// featured force pass: 7/8 of those blocks, 72 registers).  Shapes 3-5 stage
-// the candidates in shared memory (sph_walk_tile.cuh) with 128 or 256
-// threads and room for kTileDensSlots / kTileForceSlots candidates per CTA.
+// Launch shapes of the two walks: threads per block and the form of each
+// walk.  Density: 0 = one particle per thread over global memory
+// (density_item), 1 = candidates staged in shared memory (k_density_tile),
+// 2 = staged as interleaved pairs (k_density_pairs).  Force: 0 = global
+// memory, row masks two bits at a time (force_item), 1 = staged
+// (k_force_tile), 2 = global memory, one cell field at a time
+// (k_force_fields).  The global forms run 64, 128 or 256 threads at 64
+// registers (the featured force pass: 7/8 of those blocks, 72 registers).
 // sph_autotune picks one per handle by timing them on the handle's own
 // scenes; without neighbour masks (maxParInCell > 16) every shape walks
-// global memory.
-constexpr int kWalkShapes = 6;
-constexpr int kWalkBlocks[kWalkShapes] = {64, 128, 256, 128, 256, 128};
-constexpr bool kWalkTiled[kWalkShapes] = {false, false, false, true, true, true};
-constexpr uint32_t kTileDensSlots[kWalkShapes] = {0, 0, 0, 2048, 4096, 1024};
-constexpr uint32_t kTileForceSlots[kWalkShapes] = {0, 0, 0, 1536, 2560, 768};
-constexpr int kDefaultShape = 1;
+// global memory, one particle per thread, unmasked.
+struct WalkShape {
+  int threads, dens, force;
+};
+constexpr int kWalkShapes = 9;
+constexpr WalkShape kShapes[kWalkShapes] = {
+    {64, 0, 0}, {128, 0, 0}, {256, 0, 0}, {128, 1, 1}, {128, 2, 2},
+    {256, 2, 2}, {128, 2, 0}, {128, 0, 2}, {64, 2, 2}};
+constexpr uint32_t kTileDensSlots = 2048, kTileForceSlots = 1536;  // shape 3
+constexpr uint32_t kPairs64 = 512, kPairs128 = 896, kPairs256 = 1792;  // k_density_pairs
+constexpr int kDefaultShape = 4;
 static_assert(kWalkShapes == SPH_WALK_SHAPES, "walk shapes in pibiti_sph.h");
 
 // Neighbour masks: with maxParInCell <= 16, the density pass records for
@@ -422,7 +428,7 @@ __device__ __forceinline__ void force_item(const SceneDesc* __restrict__ sc,
       if (!m) continue;
       // cell starts by field (dx + 1); a field outside the grid holds no bit
       const uint32_t row = d.c_off + (uint32_t)(z * (int)p.gridSize_yx + y * gx) + (uint32_t)cx;
-      const uint32_t s0 = cx > 0 ? ld<kNC>(start + row - 1) : 0u;
+      const uint32_t s0 = cx > 0 ? ld<kNC>(start + (row - 1)) : 0u;
       const uint32_t s1 = ld<kNC>(start + row);
       const uint32_t s2 = cx + 1 < gx ? ld<kNC>(start + row + 1) : 0u;
       int cur = -1;
@@ -1103,7 +1109,7 @@ struct SphSystem {
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // graph_steps steps, keyed by cp at launch
   uint32_t graph_steps = 2;                         // steps per captured graph (even)
-  int walk_shape = kDefaultShape;                   // index into kWalkBlocks
+  int walk_shape = kDefaultShape;                   // index into kShapes
   // learned corrector
   SceneDesc* d_coarse = nullptr;     // scene table with timeStep * coarse_sub
   uint32_t coarse_sub = 0;
@@ -1208,62 +1214,89 @@ void launch_walks_shape(SphSystem* s, cudaStream_t st, int b, int v, const StepO
 
 inline size_t tile_smem_density(uint32_t slots) { return sizeof(TileTables) + 3 * sizeof(float) * slots; }
 inline size_t tile_smem_force(uint32_t slots) { return sizeof(TileTables) + 2 * sizeof(float4) * slots; }
+inline size_t tile_smem_pairs(uint32_t pairs) { return sizeof(TileTables) + (sizeof(float4) + sizeof(float2)) * pairs; }
 
-// Staged walks (shapes 3-5).  The featured force pass of the learned step
-// keeps the global-memory walk.
+template <int kThreads>
+constexpr uint32_t pairs_cap() { return kThreads == 64 ? kPairs64 : (kThreads == 256 ? kPairs256 : kPairs128); }
+
 template <int kThreads, class Mark>
-void launch_walks_tile(SphSystem* s, cudaStream_t st, int b, int v, const StepOpts& o, Mark& mark,
-                       uint32_t dslots, uint32_t fslots) {
+void launch_density(SphSystem* s, cudaStream_t st, int b, const StepOpts& o, int kind, Mark& mark) {
   const unsigned g = grid_for(s->N, kThreads);
-  k_density_tile<kThreads><<<g, kThreads, tile_smem_density(dslots), st>>>(
-      o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->start, s->count, s->dens, s->pres, s->dp, s->masks,
-      s->flags, dslots);
+  constexpr int kMin = 1024 / kThreads;
+  if (kind == 1 && kThreads == 128)
+    k_density_tile<128><<<g, 128, tile_smem_density(kTileDensSlots), st>>>(
+        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->start, s->count, s->dens, s->pres, s->dp, s->masks,
+        s->flags, kTileDensSlots);
+  else if (kind == 2)
+    k_density_pairs<kThreads, pairs_cap<kThreads>()><<<g, kThreads, tile_smem_pairs(pairs_cap<kThreads>()), st>>>(
+        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->start, s->count, s->dens, s->pres, s->dp, s->masks,
+        s->flags);
+  else
+    k_density<true, kThreads, kMin><<<g, kThreads, 0, st>>>(o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->start,
+                                                            s->count, s->dens, s->pres, s->dp, s->masks, s->flags);
   mark();
-  if (o.feat)
+}
+
+template <int kThreads>
+void launch_force(SphSystem* s, cudaStream_t st, int b, int v, const StepOpts& o, int kind) {
+  const unsigned g = grid_for(s->N, kThreads);
+  constexpr int kMin = 1024 / kThreads;
+  if (o.feat)  // the featured pass of the learned step: the global row walk
     k_force<true, 128, 8, true><<<grid_for(s->N, 128), 128, 0, st>>>(
         o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->dp, s->start, s->count,
         s->masks, s->vel[v], o.fo);
-  else
-    k_force_tile<kThreads><<<g, kThreads, tile_smem_force(fslots), st>>>(
+  else if (kind == 1 && kThreads == 128)
+    k_force_tile<128><<<g, 128, tile_smem_force(kTileForceSlots), st>>>(
         o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->dp, s->start, s->count,
-        s->masks, s->vel[v], fslots);
+        s->masks, s->vel[v], kTileForceSlots);
+  else if (kind == 2)
+    k_force_fields<kThreads, kMin><<<g, kThreads, 0, st>>>(o.scenes, s->d_poff, s->S, s->N, s->pos[b],
+                                                           s->vel[1 - v], s->dp, s->start, s->masks, s->vel[v]);
+  else
+    k_force<true, kThreads, kMin, false><<<g, kThreads, 0, st>>>(
+        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->dp, s->start, s->count,
+        s->masks, s->vel[v], o.fo);
 }
 
 template <bool kMask, class Mark>
 void launch_walks(SphSystem* s, cudaStream_t st, int b, int v, const StepOpts& o, Mark& mark) {
-  const int shape = s->walk_shape;
-  if (kMask && kWalkTiled[shape]) {
-    if (kWalkBlocks[shape] == 256)
-      launch_walks_tile<256>(s, st, b, v, o, mark, kTileDensSlots[shape], kTileForceSlots[shape]);
-    else
-      launch_walks_tile<128>(s, st, b, v, o, mark, kTileDensSlots[shape], kTileForceSlots[shape]);
+  const WalkShape& w = kShapes[s->walk_shape];
+  if (kMask) {
+    switch (w.threads) {
+      case 64:
+        launch_density<64>(s, st, b, o, w.dens, mark);
+        launch_force<64>(s, st, b, v, o, w.force);
+        break;
+      case 256:
+        launch_density<256>(s, st, b, o, w.dens, mark);
+        launch_force<256>(s, st, b, v, o, w.force);
+        break;
+      default:
+        launch_density<128>(s, st, b, o, w.dens, mark);
+        launch_force<128>(s, st, b, v, o, w.force);
+        break;
+    }
     return;
   }
-  switch (kWalkBlocks[shape]) {
-    case 64: launch_walks_shape<kMask, 64, 16>(s, st, b, v, o, mark); break;
-    case 256: launch_walks_shape<kMask, 256, 4>(s, st, b, v, o, mark); break;
-    default: launch_walks_shape<kMask, 128, 8>(s, st, b, v, o, mark); break;
+  switch (w.threads) {
+    case 64: launch_walks_shape<false, 64, 16>(s, st, b, v, o, mark); break;
+    case 256: launch_walks_shape<false, 256, 4>(s, st, b, v, o, mark); break;
+    default: launch_walks_shape<false, 128, 8>(s, st, b, v, o, mark); break;
   }
 }
 
 // Shared memory the staged walks may use (set once per handle).
 int tile_attributes() {
-  size_t dmax128 = 0, fmax128 = 0, dmax256 = 0, fmax256 = 0;
-  for (int k = 0; k < kWalkShapes; ++k) {
-    if (!kWalkTiled[k]) continue;
-    size_t& dm = kWalkBlocks[k] == 256 ? dmax256 : dmax128;
-    size_t& fm = kWalkBlocks[k] == 256 ? fmax256 : fmax128;
-    dm = std::max(dm, tile_smem_density(kTileDensSlots[k]));
-    fm = std::max(fm, tile_smem_force(kTileForceSlots[k]));
-  }
-  SPH_CUDA(cudaFuncSetAttribute(k_density_tile<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dmax128),
-           "staged density walk shared memory");
-  SPH_CUDA(cudaFuncSetAttribute(k_density_tile<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dmax256),
-           "staged density walk shared memory");
-  SPH_CUDA(cudaFuncSetAttribute(k_force_tile<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fmax128),
-           "staged force walk shared memory");
-  SPH_CUDA(cudaFuncSetAttribute(k_force_tile<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fmax256),
-           "staged force walk shared memory");
+  SPH_CUDA(cudaFuncSetAttribute(k_density_tile<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tile_smem_density(kTileDensSlots)), "staged density walk shared memory");
+  SPH_CUDA(cudaFuncSetAttribute(k_force_tile<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tile_smem_force(kTileForceSlots)), "staged force walk shared memory");
+  SPH_CUDA(cudaFuncSetAttribute(k_density_pairs<64, kPairs64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tile_smem_pairs(kPairs64)), "staged density walk shared memory");
+  SPH_CUDA(cudaFuncSetAttribute(k_density_pairs<128, kPairs128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tile_smem_pairs(kPairs128)), "staged density walk shared memory");
+  SPH_CUDA(cudaFuncSetAttribute(k_density_pairs<256, kPairs256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tile_smem_pairs(kPairs256)), "staged density walk shared memory");
   return SPH_OK;
 }
 
@@ -1684,7 +1717,7 @@ int sph_set_walk_shape(SphSystem* s, uint32_t shape) {
 int sph_get_walk_shape(SphSystem* s, uint32_t* shape, uint32_t* threads) {
   if (!s) return fail(SPH_ERR_ARG, "null handle");
   if (shape) *shape = (uint32_t)s->walk_shape;
-  if (threads) *threads = (uint32_t)kWalkBlocks[s->walk_shape];
+  if (threads) *threads = (uint32_t)kShapes[s->walk_shape].threads;
   return SPH_OK;
 }
 

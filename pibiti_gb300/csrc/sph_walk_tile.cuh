@@ -433,3 +433,219 @@ k_force_tile(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff
   vel_out[i] = make_float4(__fadd_rn(vi.x, add.x), __fadd_rn(vi.y, add.y), __fadd_rn(vi.z, add.z),
                            __fadd_rn(vi.w, 0.f));
 }
+
+// ---- density, second form: interleaved candidate pairs ------------------------
+// Slots in pairs: pair q holds (x, x', y, y') in one float4 and (z, z') in one
+// float2, so a thread loads two candidates with two shared-memory loads.  The
+// capacity is a compile-time constant (the z array sits at a fixed offset).
+// Per pair of candidates: the squared distances and h^2 - r^2 as FP32 pairs,
+// max(h^2 - r^2, 0) by a saturating FMA (exact for h^2 <= 1: a positive
+// difference below 1 is unchanged, a negative one or NaN becomes +0), and
+// the mask bits from the sign bits of h2_out - r^2 shifted in with funnel
+// shifts (sign set = outside; the field keeps the complement, so a NaN
+// distance, whose difference has a clear sign bit, stays in the mask as
+// !(r2 >= h2_out) keeps it).  A squared distance equal to h2_out also stays
+// in: the mask only has to hold every pair the force pass can use, and the
+// force term itself rejects r >= h.
+
+__device__ __forceinline__ float fma_sat(float a, float b, float c) {
+  float d;
+  asm("fma.rn.sat.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+template <int kThreads, uint32_t kPairs>
+__global__ void __launch_bounds__(kThreads, 1024 / kThreads)
+k_density_pairs(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
+                const float4* __restrict__ pos, const uint32_t* __restrict__ start,
+                const uint32_t* __restrict__ count, float* __restrict__ dens_out,
+                float* __restrict__ pres_out, float2* __restrict__ dp_out,
+                unsigned long long* __restrict__ masks, uint32_t* __restrict__ flags) {
+  extern __shared__ __align__(16) unsigned char tile_smem[];
+  TileTables& t = *reinterpret_cast<TileTables*>(tile_smem);
+  float4* sXY = reinterpret_cast<float4*>(tile_smem + sizeof(TileTables));
+  float2* sZ = reinterpret_cast<float2*>(sXY + kPairs);
+  const uint32_t i0 = blockIdx.x * kThreads, i = i0 + threadIdx.x;
+  const bool valid = i < N;
+  float4 xi = make_float4(0.f, 0.f, 0.f, 0.f);
+  int3 g = make_int3(0, 0, 0);
+  const SceneDesc& d0 = sc[S == 1 ? 0 : scene_of(poff, S, valid ? i : N - 1)];
+  if (valid) {
+    xi = __ldg(pos + i);
+    const int3 r = grid_pos(d0.p, xi);
+    g = make_int3(min(max(r.x, 0), (int)d0.p.gridSize.x - 1), min(max(r.y, 0), (int)d0.p.gridSize.y - 1),
+                  min(max(r.z, 0), (int)d0.p.gridSize.z - 1));
+  }
+  // the saturating form needs h^2 <= 1 (uniform: one scene per staged block)
+  const bool ok = tile_setup<kThreads, true>(sc, poff, S, N, i0, i, g, start, count, 2 * kPairs, t) &&
+                  sc[t.h.scene].p.h2 <= 1.f;
+  if (!ok) {
+    if (valid) density_item<true>(sc, poff, S, N, pos, start, count, dens_out, pres_out, dp_out, masks, flags, i);
+    return;
+  }
+  const TileHead h = t.h;
+  const SimParams& p = sc[h.scene].p;
+  {
+    float* xy = reinterpret_cast<float*>(sXY);
+    float* zz = reinterpret_cast<float*>(sZ);
+    const uint32_t lane = threadIdx.x & 31, half = lane >> 4, k = lane & 15;
+    for (uint32_t c = 2 * (threadIdx.x >> 5) + half; c < h.nb; c += 2 * (kThreads / 32)) {
+      const uint32_t o = t.off[c], np = t.off[c + 1] - o;
+      if (k < np) {
+        float4 x = make_float4(kTileDummy, kTileDummy, kTileDummy, 0.f);
+        if (k < t.n[c]) x = __ldg(pos + t.src[c] + k);
+        const uint32_t s = o + k, q = s >> 1, e = s & 1;
+        xy[4 * q + e] = x.x;
+        xy[4 * q + 2 + e] = x.y;
+        zz[2 * q + e] = x.z;
+      }
+    }
+  }
+  if (threadIdx.x == 0 && h.trunc) atomicOr(flags, 1u);
+  __syncthreads();
+  if (!valid) return;
+  const int gx = (int)p.gridSize.x, gy = (int)p.gridSize.y, gz = (int)p.gridSize.z;
+  const float2 nx = make_float2(-xi.x, -xi.x), ny = make_float2(-xi.y, -xi.y),
+               nz = make_float2(-xi.z, -xi.z);
+  const float h2 = p.h2, h2o = h2_out_of(p);
+  const float2 h2o2 = make_float2(h2o, h2o), m1 = make_float2(-1.f, -1.f);
+  float sum = 0.f;
+  // pairs q0..q1-1 of one cell's run; `out` collects one bit per slot, the
+  // first slot highest, set when the candidate lies beyond h2_out
+  auto run = [&](auto self_tag, uint32_t q0, uint32_t q1, uint32_t qs, uint32_t es, float& cell,
+                 uint32_t& out) {
+    constexpr bool kSelf = decltype(self_tag)::value;
+#pragma unroll 2
+    for (uint32_t q = q0; q < q1; ++q) {
+      const float4 a = sXY[q];
+      const float2 zq = sZ[q];
+      const float2 dx = __fadd2_rn(make_float2(a.x, a.y), nx);
+      const float2 dy = __fadd2_rn(make_float2(a.z, a.w), ny);
+      const float2 dz = __fadd2_rn(zq, nz);
+      float2 r2 = __fmul2_rn(dx, dx);
+      r2 = __ffma2_rn(dy, dy, r2);
+      r2 = __ffma2_rn(dz, dz, r2);
+      const float2 e = __ffma2_rn(m1, r2, h2o2);
+      float c0 = fma_sat(-1.f, r2.x, h2), c1 = fma_sat(-1.f, r2.y, h2);
+      uint32_t u0 = __float_as_uint(e.x), u1 = __float_as_uint(e.y);
+      if constexpr (kSelf) {
+        if (q == qs) {  // this particle: no term, no bit
+          if (es == 0) {
+            c0 = 0.f;
+            u0 = 0x80000000u;
+          } else {
+            c1 = 0.f;
+            u1 = 0x80000000u;
+          }
+        }
+      }
+      const float2 cc = __fmul2_rn(make_float2(c0, c1), make_float2(c0, c1));
+      cell = __fmaf_rn(cc.x, c0, cell);
+      cell = __fmaf_rn(cc.y, c1, cell);
+      out = __funnelshift_l(u0, out, 1);
+      out = __funnelshift_l(u1, out, 1);
+    }
+  };
+#pragma unroll 1
+  for (int r = 0; r < kRows; ++r) {
+    const int z = g.z + r / 3 - 1, y = g.y + r % 3 - 1;
+    unsigned long long rowmask = 0;
+    if (z >= 0 && z < gz && y >= 0 && y < gy) {
+      const int lrow = ((z - h.z0) * h.by + (y - h.y0)) * h.bx - h.x0;
+#pragma unroll 1
+      for (int f = 0; f < 3; ++f) {
+        const int x = g.x - 1 + f;
+        if (x < 0 || x >= gx) continue;
+        const uint32_t c = (uint32_t)(lrow + x);
+        const uint32_t o0 = t.off[c], o1 = t.off[c + 1], n = t.n[c];
+        float cell = 0.f;
+        uint32_t out = 0;
+        if (r == 4 && f == 1) {
+          const uint32_t ks = i - t.src[c];  // this particle's place in the cell
+          const uint32_t s = ks < n ? o0 + ks : 0xffffffffu;
+          run(std::true_type{}, o0 >> 1, o1 >> 1, s >> 1, s & 1, cell, out);
+        } else {
+          run(std::false_type{}, o0 >> 1, o1 >> 1, 0xffffffffu, 0u, cell, out);
+        }
+        sum = __fadd_rn(sum, cell);
+        // in-bits of the run's real candidates, candidate 0 at bit 15
+        const uint32_t np = o1 - o0;
+        uint32_t field = np ? ((~out << (16 - np)) & (0xFFFFu << (16 - n))) & 0xFFFFu : 0u;
+        rowmask |= (unsigned long long)field << (16 * (2 - f));
+      }
+    }
+    masks[(size_t)r * N + i] = rowmask;
+  }
+  const float dens = __fmul_rn(__fmul_rn(sum, p.Poly6Kern), p.particleMass);
+  const float pres = __fmul_rn(__fsub_rn(dens, p.restDensity), p.stiffness);
+  dens_out[i] = dens;
+  pres_out[i] = pres;
+  dp_out[i] = make_float2(__frcp_rn(dens), pres);
+}
+
+// ---- force, by cell fields ----------------------------------------------------
+// The masked walk of force_item, taken one cell (one 16-bit field of a row
+// mask) at a time: the cell's start is loaded once, its set bits are taken
+// highest first with 32-bit operations, and its partial sum is added to the
+// total when its bits are done (a cell without a set bit would add +0, which
+// changes nothing, so it is skipped).
+template <int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+k_force_fields(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
+               const float4* __restrict__ pos, const float4* __restrict__ vel,
+               const float2* __restrict__ dp, const uint32_t* __restrict__ start,
+               const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out) {
+  const uint32_t i = regrouped_particle<kThreads>(sc, poff, S, N, pos);
+  if (i >= N) return;
+  const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
+  const SimParams& p = d.p;
+  const float4 xi = __ldg(pos + i), vi = __ldg(vel + i);
+  const float2 dpi = __ldg(dp + i);
+  const float inv_di = dpi.x, pi = dpi.y;
+  const ForceConsts k = force_consts(p);
+  const int3 g0 = grid_pos(p, xi);
+  const int gx = (int)p.gridSize.x, gy = (int)p.gridSize.y, gz = (int)p.gridSize.z;
+  const int cx = min(max(g0.x, 0), gx - 1), cy = min(max(g0.y, 0), gy - 1), cz = min(max(g0.z, 0), gz - 1);
+  float3 F = make_float3(0.f, 0.f, 0.f);
+  unsigned long long mnext = masks[i];
+#pragma unroll 1
+  for (int r = 0; r < kRows; ++r) {
+    const unsigned long long m = mnext;
+    if (r + 1 < kRows) mnext = masks[(size_t)(r + 1) * N + i];
+    if (!m) continue;
+    const int z = cz + r / 3 - 1, y = cy + r % 3 - 1;
+    const int row = z * (int)p.gridSize_yx + y * gx + cx;  // the cell at dx = 0
+#pragma unroll 1
+    for (int f = 0; f < 3; ++f) {
+      uint32_t bits = (uint32_t)(m >> (16 * (2 - f))) & 0xFFFFu;
+      if (!bits) continue;
+      // the cell at dx = f - 1 (a field outside the grid holds no bit); its
+      // index is formed before the pointer, so the cell at dx = -1 of the
+      // grid's first cell never becomes a 2^32-element pointer offset
+      const uint32_t c = d.c_off + (uint32_t)(row + f - 1);
+      const uint32_t s0 = __ldg(start + c) + 15u;
+      float3 cell = make_float3(0.f, 0.f, 0.f);
+      do {
+        const int b = 31 - __clz(bits);
+        bits ^= 1u << b;
+        const uint32_t j = s0 - (uint32_t)b;  // candidate 15 - b
+        const float4 xj = __ldg(pos + j), vj = __ldg(vel + j);
+        const float2 dpj = __ldg(dp + j);
+        const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
+        const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
+        float3 t;
+        if (force_term(k, vi, inv_di, pi, vj, dpj.x, dpj.y, rx, ry, rz, dist2, t)) {
+          cell.x = __fadd_rn(cell.x, t.x);
+          cell.y = __fadd_rn(cell.y, t.y);
+          cell.z = __fadd_rn(cell.z, t.z);
+        }
+      } while (bits);
+      F.x = __fadd_rn(F.x, cell.x);
+      F.y = __fadd_rn(F.y, cell.y);
+      F.z = __fadd_rn(F.z, cell.z);
+    }
+  }
+  const float3 add = velocity_increment(p, F, xi, vi);
+  vel_out[i] = make_float4(__fadd_rn(vi.x, add.x), __fadd_rn(vi.y, add.y), __fadd_rn(vi.z, add.z),
+                           __fadd_rn(vi.w, 0.f));
+}

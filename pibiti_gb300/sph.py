@@ -291,8 +291,9 @@ class SPH:
         """update(k) as one cooperative launch of k steps (same results)."""
         check(lib().sph_set_persistent(self._h, int(on)))
 
-    WALK_THREADS = (64, 128, 256, 128, 256, 128)  # by shape (sph_set_walk_shape)
-    WALK_STAGED = (False, False, False, True, True, True)
+    # by shape (sph_set_walk_shape): threads per block, staged density walk
+    WALK_THREADS = (64, 128, 256, 128, 128, 256, 128, 128, 64)
+    WALK_STAGED = (False, False, False, True, True, True, True, False, True)
 
     def set_walk_shape(self, shape: int) -> None:
         check(lib().sph_set_walk_shape(self._h, shape))

@@ -288,6 +288,13 @@ def test_staged_walks_match_global_walks_on_sparse_particles(cuda):
     pos = w.pos.copy()
     pos[:, :3] = rng.uniform(0.05, 0.95, size=(len(pos), 3)).astype(np.float32)
     pos[:2048, :3] = pos[:2048, :3] * 0.2 + 0.1  # a crowded corner too
+    # and particles in the grid's first cells along every axis (their
+    # neighbour cells at -1 lie outside the grid; cell 0 itself stays empty)
+    cs = p.cellSize.x
+    edge = rng.uniform(0.2, 0.8, size=(256, 3)).astype(np.float32) * cs
+    edge[:128, 0] += cs  # cells (1, 0, 0)
+    edge[128:, 1] += cs  # cells (0, 1, 0)
+    pos[2048:2304, :3] = edge
     vel = rng.normal(0.0, 0.5, size=pos.shape).astype(np.float32)
     outs = []
     for shape in range(len(SPH.WALK_THREADS)):
