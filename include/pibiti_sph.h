@@ -7,7 +7,7 @@
  *
  *  1. Stage entry points with the argument lists of the reference's own
  *     extern "C" wrappers (source/CUDA/System.cuh:1-38,
- *     source/CUDA/radixsort.cuh:67-69), with OpenGL buffer ids replaced by
+ *     source/CUDA/radixsort.cuh:30-32), with OpenGL buffer ids replaced by
  *     device pointers.  A program that called the reference's wrappers calls
  *     these in the same order (cSPH::Update, source/SPH/SPH_Update.cpp:12-81)
  *     and gets the same buffers back.  Device buffers belong to the caller.
@@ -81,7 +81,7 @@ int sph_integrate(const sph_float4* oldPos, sph_float4* newPos, const sph_float4
 /* calcHash (System.cuh:27): particleHash[i] = {cell hash of pos[i], i}. */
 int sph_calcHash(const sph_float4* pos, sph_uint2* particleHash, int numParticles);
 
-/* RadixSort (radixsort.cuh:67-69, radixsort_kernel.cu:445-472): stable sort
+/* RadixSort (radixsort.cuh:30-32, radixsort_kernel.cu:445-472): stable sort
    of (key, value) pairs by the low `bits` bits of the key, 8 bits per pass,
    ping-ponging between pData0 and pData1.  After an even number of passes
    (bits = 16 or 32, the values cSPH::Update uses) the result is in pData0;
@@ -93,9 +93,12 @@ int sph_RadixSort(sph_uint2* pData0, sph_uint2* pData1, uint32_t elements, uint3
    run (a frame loop that cannot absorb cudaFree's device-wide wait, or a
    process whose device memory is held by another allocator).  Its scratch
    is a 2.0 MiB array inside the library that every GPU loading it keeps
-   until exit, so at most 4,194,304 pairs (larger: SPH_ERR_ARG).  The first
-   call on a device looks up the array's address, so make it before any
-   stream capture; calls that overlap on the GPU share the array and race.
+   until exit, so at most 4,194,304 pairs (larger: SPH_ERR_ARG).  Each call
+   outside a stream capture looks up the array's address on the current
+   device (so a cudaDeviceReset in between is harmless); a call inside a
+   capture uses the address of the last call on that device, so make one
+   before capturing (else SPH_ERR_STATE).  Calls that overlap on the GPU
+   share the array and race.
    Runs on the stage stream; result location as sph_RadixSort. */
 int sph_RadixSort_noalloc(sph_uint2* pData0, sph_uint2* pData1, uint32_t elements, uint32_t bits);
 

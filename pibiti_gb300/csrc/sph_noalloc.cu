@@ -13,9 +13,12 @@
 // (2.0 MiB), which every GPU that loads this library holds until the process
 // exits.  That covers sorts of up to kNoAllocMaxElements (4,194,304) pairs;
 // larger requests are refused with SPH_ERR_ARG.  The device address of the
-// array is looked up with cudaGetSymbolAddress on the first call on each
-// device (with that device current); make that first call before capturing
-// any stream.  All calls share the one array and it keeps whatever the last
+// array is looked up with cudaGetSymbolAddress (with the device current) on
+// every call made outside a stream capture, and kept per device for calls
+// made inside one: make one call on each device before capturing any stream.
+// Looking it up again outside captures keeps the address right after a
+// cudaDeviceReset, which reloads the module.  All calls share the one array
+// and it keeps whatever the last
 // call left there: the sort writes every histogram and offset entry before it
 // reads them, and the scan's one counter word is cleared on the stream before
 // each use.  Calls whose work overlaps on the GPU (two host threads, or two
@@ -40,16 +43,21 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 uint32_t* g_scratch_addr[kMaxDevices] = {};
 
-// Device address of g_radix_scratch on the current device (looked up once).
-int scratch_address(uint32_t** out) {
+// Device address of g_radix_scratch on the current device: looked up when
+// `stream` is not capturing (and kept), the kept one while it is.
+int scratch_address(cudaStream_t stream, uint32_t** out) {
   int dev = 0;
   SPH_CUDA(cudaGetDevice(&dev), "RadixSort_noalloc: current device");
   if (dev < 0 || dev >= kMaxDevices) return fail(SPH_ERR_ARG, "RadixSort_noalloc: device %d", dev);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  SPH_CUDA(cudaStreamIsCapturing(stream, &cap), "RadixSort_noalloc: capture status");
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_addr[dev]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     SPH_CUDA(cudaGetSymbolAddress(&p, g_radix_scratch), "RadixSort_noalloc: scratch address");
     g_scratch_addr[dev] = static_cast<uint32_t*>(p);
+  } else if (!g_scratch_addr[dev]) {
+    return fail(SPH_ERR_STATE, "RadixSort_noalloc: first call on device %d inside a stream capture", dev);
   }
   *out = g_scratch_addr[dev];
   return SPH_OK;
@@ -73,7 +81,8 @@ extern "C" int sph_RadixSort_noalloc(sph_uint2* pData0, sph_uint2* pData1, uint3
                 elements, kNoAllocMaxElements);
   if (radix_scratch_words(elements) > kNoAllocWords)
     return fail(SPH_ERR_ARG, "RadixSort_noalloc: scratch too small for %u pairs", elements);
+  const cudaStream_t st = stage_stream();
   uint32_t* scratch = nullptr;
-  SPH_TRY(scratch_address(&scratch));
-  return radix_sort_pairs((uint2*)pData0, (uint2*)pData1, elements, bits, scratch, stage_stream());
+  SPH_TRY(scratch_address(st, &scratch));
+  return radix_sort_pairs((uint2*)pData0, (uint2*)pData1, elements, bits, scratch, st);
 }

@@ -1,8 +1,8 @@
 """sph_RadixSort_noalloc, the sort for callers that cannot allocate device
 memory while they run (its scratch is a fixed array inside the library),
-against the existing sph_RadixSort through the C ABI: two calls in a row,
-each compared bit for bit (an integer sort has no tolerance), plus the
-refusal of sizes beyond the array's 4,194,304-pair limit.
+against the existing sph_RadixSort through the C ABI: calls in a row, each
+compared bit for bit (an integer sort has no tolerance), the last two at the
+array's 4,194,304-pair limit, plus the refusal of larger sizes.
 
 The file name makes pytest collect it last, so a run that stops at the first
 failure has run every other test before this one."""
@@ -38,7 +38,9 @@ def test_noalloc_matches_radix_sort_twice(cuda):
     torch = cuda
     from pibiti_gb300 import _lib
     L = _lib.lib()
-    for call, (n, bits, seed) in enumerate([(1_048_576, 32, 1), (300_001, 24, 2)]):
+    # the last two calls fill the whole array (an odd pass count at 24 bits)
+    cases = [(1_048_576, 32, 1), (300_001, 24, 2), (MAX_PAIRS, 32, 3), (MAX_PAIRS, 24, 4)]
+    for call, (n, bits, seed) in enumerate(cases):
         kv = _pairs(torch, n, seed)
         ref = _sort(torch, L.sph_RadixSort, kv, bits)
         got = _sort(torch, L.sph_RadixSort_noalloc, kv, bits)
