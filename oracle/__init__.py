@@ -55,6 +55,8 @@ def lib() -> ctypes.CDLL:
         L.orc_integrate_f64.argtypes = [vp, _f32p, _f32p, u32, _f64p, _f64p]
         L.orc_step_f32.argtypes = [vp, _f32p, _f32p, u32, u32, ctypes.c_int]
         L.orc_step_f32.restype = ctypes.c_int
+        L.orc_step_d64.argtypes = [vp, _f64p, _f64p, u32, u32, _f64p]
+        L.orc_step_d64.restype = ctypes.c_int
         L.orc_threads.restype = ctypes.c_int
         L.orc_reduce.argtypes = [vp, _f32p, _f32p, u32, _f64p]
         _lib = L
@@ -189,6 +191,20 @@ def step(params, pos, vel, steps: int = 1, threads: int = 0):
     if rc != 0:
         raise MemoryError("oracle step could not allocate its work buffers")
     return pos, vel
+
+
+def step_fp64(params, pos, vel, steps: int = 1, with_density: bool = False):
+    """Whole steps with the state held in double precision (orc_step_d64);
+    returns new (pos, vel) as float64 arrays, and with `with_density` the
+    mean density of the last step as a third item."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 4).copy()
+    vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1, 4).copy()
+    md = np.zeros(1, np.float64)
+    rc = lib().orc_step_d64(_pb(params), _p(pos, ctypes.c_double), _p(vel, ctypes.c_double),
+                            len(pos), steps, _p(md, ctypes.c_double))
+    if rc != 0:
+        raise MemoryError("oracle step could not allocate its work buffers")
+    return (pos, vel, float(md[0])) if with_density else (pos, vel)
 
 
 def threads() -> int:

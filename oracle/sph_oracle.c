@@ -45,6 +45,20 @@ static inline void grid_pos(const SimParams* p, const float* pos4, int g[3]) {
   g[2] = f2i_sat(floorf(gz));
 }
 
+/* The same cell lookup for positions held in double (the double-precision
+   trajectory): floor((p - worldMin) / cellSize) in double. */
+static inline int32_t f2i_sat_d(double f) {
+  if (f != f) return 0;
+  if (f >= 2147483648.0) return INT32_MAX;
+  if (f < -2147483648.0) return INT32_MIN;
+  return (int32_t)f;
+}
+static inline void grid_pos_d(const SimParams* p, const double* pos4, int g[3]) {
+  g[0] = f2i_sat_d(floor((pos4[0] - (double)p->worldMin.x) / (double)p->cellSize.x));
+  g[1] = f2i_sat_d(floor((pos4[1] - (double)p->worldMin.y) / (double)p->cellSize.y));
+  g[2] = f2i_sat_d(floor((pos4[2] - (double)p->worldMin.z) / (double)p->cellSize.z));
+}
+
 /* calcGridHash (Kernel_Cell.cui:15-19): z * (gx*gy) + y * gx + x with
    24-bit multiplies; out-of-grid coordinates wrap exactly as there. */
 static inline uint32_t grid_hash(const SimParams* p, int x, int y, int z) {
@@ -70,6 +84,8 @@ static inline uint32_t fetch_key(const uint32_t* kv, uint32_t n, uint32_t j) {
 
 /* ---- floating-point stages, instantiated per precision ---------------- */
 #define REAL float
+#define PIN float
+#define GRID_POS grid_pos
 #define SFX(name) name##_f32
 #define FMA(a, b, c) fmaf((a), (b), (c))
 #define SQRT(a) sqrtf(a)
@@ -86,8 +102,12 @@ static inline uint32_t fetch_key(const uint32_t* kv, uint32_t n, uint32_t j) {
 #undef COS
 #undef ATAN
 #undef FABS
+#undef PIN
+#undef GRID_POS
 
 #define REAL double
+#define PIN float
+#define GRID_POS grid_pos
 #define SFX(name) name##_f64
 #define FMA(a, b, c) fma((a), (b), (c))
 #define SQRT(a) sqrt(a)
@@ -96,8 +116,17 @@ static inline uint32_t fetch_key(const uint32_t* kv, uint32_t n, uint32_t j) {
 #define ATAN(a) atan(a)
 #define FABS(a) fabs(a)
 #include "sph_oracle_core.inc"
+#undef SFX
+#undef PIN
+#undef GRID_POS
+#define PIN double
+#define GRID_POS grid_pos_d
+#define SFX(name) name##_d64
+#include "sph_oracle_core.inc"
 #undef REAL
 #undef SFX
+#undef PIN
+#undef GRID_POS
 #undef FMA
 #undef SQRT
 #undef SIN
@@ -433,6 +462,81 @@ done:
 #ifdef _OPENMP
   omp_set_num_threads(saved);
 #endif
+  return rc;
+}
+
+/* cSPH::Update (SPH_Update.cpp:12-81) with the whole state in double:
+   integrate, cell of each position (double, clamped into the grid), stable
+   sort by (cell, index), reorder, density, force.  The reference trajectory
+   a single-precision run is measured against; every arithmetic step is the
+   restatement of the single-precision oracle evaluated in double.
+   *mean_density (if not NULL) gets the mean of the last step's densities. */
+int orc_step_d64(const SimParams* p, double* pos, double* vel, uint32_t n, uint32_t steps,
+                 double* mean_density) {
+  const size_t d4 = sizeof(double) * 4 * (size_t)n;
+  double* npos = (double*)malloc(d4);
+  double* nvel = (double*)malloc(d4);
+  double* spos = (double*)malloc(d4);
+  double* svel = (double*)malloc(d4);
+  double* dens = (double*)malloc(sizeof(double) * (size_t)n);
+  double* pres = (double*)malloc(sizeof(double) * (size_t)n);
+  uint32_t* kv = (uint32_t*)malloc(sizeof(uint32_t) * 2 * (size_t)n);
+  uint32_t* kv2 = (uint32_t*)malloc(sizeof(uint32_t) * 2 * (size_t)n);
+  uint32_t* cs = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)p->numCells + 1));
+  int rc = 0;
+  if (!npos || !nvel || !spos || !svel || !dens || !pres || !kv || !kv2 || !cs) {
+    rc = -1;
+    goto done;
+  }
+  for (uint32_t s = 0; s < steps; ++s) {
+    orc_integrate_d64(p, pos, vel, n, npos, nvel);
+    memcpy(pos, npos, d4);
+    memcpy(vel, nvel, d4);
+    memset(cs, 0, sizeof(uint32_t) * ((size_t)p->numCells + 1));
+    for (uint32_t i = 0; i < n; ++i) {
+      int g[3];
+      grid_pos_d(p, pos + 4 * (size_t)i, g);
+      for (int k = 0; k < 3; ++k) {
+        const int lim = (int)(k == 0 ? p->gridSize.x : (k == 1 ? p->gridSize.y : p->gridSize.z)) - 1;
+        g[k] = g[k] < 0 ? 0 : (g[k] > lim ? lim : g[k]);
+      }
+      kv[2 * i] = grid_hash(p, g[0], g[1], g[2]);
+      kv[2 * i + 1] = i;
+      cs[kv[2 * i] + 1]++;
+    }
+    for (uint32_t c = 0; c < p->numCells; ++c) cs[c + 1] += cs[c];
+    for (uint32_t i = 0; i < n; ++i) {
+      const uint32_t o = cs[kv[2 * i]]++;
+      kv2[2 * o] = kv[2 * i];
+      kv2[2 * o + 1] = kv[2 * i + 1];
+    }
+    memcpy(kv, kv2, sizeof(uint32_t) * 2 * (size_t)n);
+    memset(cs, 0xff, sizeof(uint32_t) * (size_t)p->numCells);
+    for (uint32_t i = 0; i < n; ++i)
+      if (i == 0 || kv[2 * i] != kv[2 * (i - 1)]) cs[kv[2 * i]] = i;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const uint32_t j = kv[2 * i + 1];
+      memcpy(spos + 4 * i, pos + 4 * (size_t)j, 32);
+      memcpy(svel + 4 * i, vel + 4 * (size_t)j, 32);
+    }
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < (int64_t)n; ++i)
+      density_one_d64(p, spos, kv, cs, n, (uint32_t)i, dens + i, pres + i, 0);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const uint32_t si = kv[2 * i + 1];
+      force_one_d64(p, spos, svel, dens, pres, kv, cs, n, (uint32_t)i, vel + 4 * (size_t)si, 0, 0);
+    }
+    if (mean_density && s + 1 == steps) {
+      double sum = 0;
+      for (uint32_t i = 0; i < n; ++i) sum += dens[i];
+      *mean_density = n ? sum / n : 0.0;
+    }
+  }
+done:
+  free(npos); free(nvel); free(spos); free(svel); free(dens); free(pres);
+  free(kv); free(kv2); free(cs);
   return rc;
 }
 

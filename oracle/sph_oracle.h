@@ -82,6 +82,14 @@ void orc_integrate_f64(const SimParams* p, const float* pos, const float* vel, u
 int orc_step_f32(const SimParams* p, float* pos, float* vel, uint32_t n, uint32_t steps,
                  int threads);
 
+/* The same steps with positions and velocities held in double and every
+   stage evaluated in double: the reference trajectory a single-precision run
+   is measured against (kinetic energy and mean-density drift).
+   *mean_density (if not NULL) gets the mean of the last step's densities.
+   Returns 0, or -1 when a work buffer could not be allocated. */
+int orc_step_d64(const SimParams* p, double* pos, double* vel, uint32_t n, uint32_t steps,
+                 double* mean_density);
+
 /* Number of OpenMP threads a parallel region would use. */
 int orc_threads(void);
 

@@ -67,22 +67,66 @@ def test_multistep_matches_oracle(cuda):
     np.testing.assert_array_equal(vel, ovel)
 
 
-def test_drift_bounds(cuda):
-    """Kinetic energy and mean density of GPU vs oracle trajectories, 300
-    steps of the 32,768-particle dam break: within 1e-4 relative."""
+# Drift of the single-precision GPU trajectory from the double-precision
+# one (oracle.step_fp64: the same step with the state and every stage in
+# double), 1000 steps of the 32,768-particle dam break, sampled every 100
+# steps.  Kinetic energy is compared against the run's largest kinetic
+# energy (it falls by an order of magnitude after the impact near step 350,
+# where the splash makes the two trajectories part); mean density relative.
+# Measured: before the impact (steps <= 300) 2.2e-4 of the peak and 3e-4
+# relative; over the whole run 3.5e-3 and 8.5e-3.
+DRIFT_EARLY_STEPS = 300
+DRIFT_KE_EARLY, DRIFT_KE_ALL = 1e-3, 1e-2      # |KE32 - KE64| / max KE64
+DRIFT_RHO_EARLY, DRIFT_RHO_ALL = 1e-3, 2e-2    # |rho32 - rho64| / rho64
+
+
+def test_drift_against_fp64_trajectory(cuda):
     w = configs.dambreak_small(side=32)
     p = Scene.parse(w.xml).params
+    ke32, rho32 = [], []
     with system_from(p, w.pos, w.vel) as s:
-        s.update(300)
-        st = s.stats()[0]
-        d_gpu, _ = s.fields()
-    opos, ovel = oracle.step(p, w.pos, w.vel, steps=300)
-    ke_o, _ = oracle.reduce(p, ovel)
-    assert abs(st[0] - ke_o) <= 1e-4 * ke_o
-    assert st[3] == 0
-    assert abs(st[1] - d_gpu.astype(np.float64).mean()) <= 1e-6 * st[1]
+        for _ in range(10):
+            s.update(100)
+            st = s.stats()[0]
+            assert st[3] == 0
+            ke32.append(st[0])
+            rho32.append(st[1])
+    ke64, rho64 = [], []
+    pos, vel = w.pos, w.vel
+    m = float(p.particleMass)
+    for _ in range(10):
+        pos, vel, md = oracle.step_fp64(p, pos, vel, steps=100, with_density=True)
+        ke64.append(0.5 * m * float((vel[:, :3] ** 2).sum()))
+        rho64.append(md)
+    ke32, rho32, ke64, rho64 = map(np.asarray, (ke32, rho32, ke64, rho64))
+    steps = 100 * np.arange(1, 11)
+    early = steps <= DRIFT_EARLY_STEPS
+    dke = np.abs(ke32 - ke64) / ke64.max()
+    drho = np.abs(rho32 - rho64) / rho64
+    assert dke[early].max() <= DRIFT_KE_EARLY, dke
+    assert dke.max() <= DRIFT_KE_ALL, dke
+    assert drho[early].max() <= DRIFT_RHO_EARLY, drho
+    assert drho.max() <= DRIFT_RHO_ALL, drho
     # k=3 is soft: the 0.73 m column compresses to about twice rest density
-    assert p.restDensity < st[1] < 4 * p.restDensity
+    assert p.restDensity < rho32[-1] < 4 * p.restDensity
+
+
+def test_stats_reductions_at_1m(cuda):
+    """The GPU's kinetic-energy and mean-density reductions after 200 steps
+    of the 1,048,576-particle double dam break, against double-precision sums
+    of the same state read back to the host."""
+    w = configs.dambreak_double()
+    p = Scene.parse(w.xml).params
+    with system_from(p, w.pos, w.vel) as s:
+        s.update(200)
+        st = s.stats()[0]
+        vel = s.get_array(ARRAY_VEL).astype(np.float64)
+        dens, _ = s.fields()
+    ke = 0.5 * float(p.particleMass) * float((vel[:, :3] ** 2).sum())
+    rho = float(dens.astype(np.float64).mean())
+    assert abs(st[0] - ke) <= 1e-5 * ke
+    assert abs(st[1] - rho) <= 1e-6 * rho
+    assert st[3] == 0
 
 
 def test_ensemble_equals_separate_runs(cuda):

@@ -119,6 +119,22 @@ def test_step_matches_stages(golden):
     np.testing.assert_array_equal(vel, o["vel"])
 
 
+def test_fp64_step_against_stages(golden):
+    """The double-precision trajectory step (oracle.step_fp64) after one step
+    equals the double-precision stages applied to the same input within the
+    rounding of the positions to float that the stages read (1e-6 relative),
+    and it stays within single-precision reach of the float step."""
+    g = golden("step_dambreak.npz")
+    p = params_from(g["params"])
+    pos64, vel64, rho = oracle.step_fp64(p, g["pos_in"], g["vel_in"], steps=1, with_density=True)
+    pos32, vel32 = oracle.step(p, g["pos_in"], g["vel_in"], steps=1)
+    scale = np.abs(vel64[:, :3]).max()
+    np.testing.assert_allclose(pos64, pos32, rtol=0, atol=1e-6)
+    np.testing.assert_allclose(vel64, vel32, rtol=0, atol=2e-5 * scale)
+    d64, _ = oracle.density(p, g["sorted_pos"], g["sorted"], g["cell_start"], fp64=True)
+    assert abs(rho - float(np.mean(d64))) <= 1e-6 * rho
+
+
 @pytest.mark.parametrize("case", ["dambreak", "features"])
 def test_live_reference(case, golden):
     """Where the reference tree is mounted, run its kernels on fresh inputs."""
