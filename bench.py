@@ -173,7 +173,7 @@ def stage_roofline(stages: dict, n: int, cells: int, peak: float, peak_kind: str
     bp, bc = STAGE_BYTES[dom]
     alg = bp * n + bc * cells
     achieved = alg / (stage_ms[dom] / 1e3) / 1e9
-    kernel = f"k_{dom}" + ("_tile" if walk.get("staged") and dom in ("density", "force") else "")
+    kernel = walk.get("kernels", {}).get(dom, f"k_{dom}")
     traffic = ncu_summary("traffic", kernel, state)
     instr = ncu_summary("instructions", kernel, state)
     binding = None
@@ -719,8 +719,9 @@ def main():
     sysm.set_array(ARRAY_POS, w.pos)
     sysm.set_array(ARRAY_VEL, w.vel)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    walk = {"shape": sysm.walk_shape(), "threads": SPH.WALK_THREADS[sysm.walk_shape()],
-            "staged": SPH.WALK_STAGED[sysm.walk_shape()]}
+    shape = sysm.walk_shape()
+    walk = {"shape": shape, "threads": SPH.WALK_THREADS[shape], "staged": SPH.WALK_STAGED[shape],
+            "kernels": dict(zip(("density", "force"), SPH.WALK_KERNELS[shape]))}
 
     with torch.cuda.stream(stream):
         sysm.update(args.warmup)

@@ -77,3 +77,14 @@ def test_invalid_params_rejected():
     with pytest.raises(_lib.SphError) as e:
         _lib.check(_lib.lib().sph_setParameters(ctypes.byref(p)))
     assert e.value.code == 3
+
+
+def test_walk_shape_tables_match_header():
+    """The Python tables of walk shapes cover exactly SPH_WALK_SHAPES shapes."""
+    import os
+    import re
+    from pibiti_gb300.sph import SPH
+    hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                            "pibiti_sph.h")).read()
+    n = int(re.search(r"#define SPH_WALK_SHAPES (\d+)", hdr).group(1))
+    assert len(SPH.WALK_THREADS) == len(SPH.WALK_STAGED) == len(SPH.WALK_KERNELS) == n
