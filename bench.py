@@ -652,6 +652,8 @@ def run_state_tool(args) -> int:
         z = np.load(args.stages)
         s.set_array(ARRAY_POS, z["pos"])
         s.set_array(ARRAY_VEL, z["vel"])
+        if args.walk_shape is not None:
+            s.set_walk_shape(args.walk_shape)
         for _ in range(args.steps):
             print(json.dumps({"stage_ms": s.step_timed()}))
     return 0
@@ -673,6 +675,8 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble measurement")
     ap.add_argument("--save-state", metavar="NPZ",
                     help="profiling aid: run --warm-steps steps of the workload, save the state, exit")
+    ap.add_argument("--walk-shape", type=int, default=None,
+                    help="profiling aid: walk shape for --stages (sph_set_walk_shape)")
     ap.add_argument("--stages", metavar="NPZ",
                     help="profiling aid: load a saved state, print --steps per-stage step times")
     ap.add_argument("--cpu-configs", action="store_true",

@@ -207,12 +207,14 @@ int sph_persistent_withheld(SphSystem* sys, uint32_t* flags);
        6     128     staged, interleaved pairs   global, row masks
        7     128     global memory               global, one cell at a time
        8      64     staged, interleaved pairs   global, one cell at a time
+       9     128     staged, interleaved pairs   global, pairs evaluated by the warp
+      10      64     staged, interleaved pairs   global, pairs evaluated by the warp
    "Staged": the candidates of the block's neighbour cells are copied to
    shared memory once per block (a block whose cells need more room, or
    whose particles belong to two scenes, walks global memory).  4 is the
    default.  Without neighbour masks (maxParInCell > 16) every shape walks
    global memory. */
-#define SPH_WALK_SHAPES 9
+#define SPH_WALK_SHAPES 11
 int sph_set_walk_shape(SphSystem* sys, uint32_t shape);
 int sph_get_walk_shape(SphSystem* sys, uint32_t* shape, uint32_t* threads_per_block);
 

@@ -188,7 +188,8 @@ k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
 // 2 = staged as interleaved pairs (k_density_pairs).  Force: 0 = global
 // memory, row masks two bits at a time (force_item), 1 = staged
 // (k_force_tile), 2 = global memory, one cell field at a time
-// (k_force_fields).  The global forms run 64, 128 or 256 threads at 64
+// (k_force_fields), 3 = global memory, pair terms evaluated by the whole
+// warp row by row (k_force_coop; 64 or 128 threads).  The global forms run 64, 128 or 256 threads at 64
 // registers (the featured force pass: 7/8 of those blocks, 72 registers).
 // sph_autotune picks one per handle by timing them on the handle's own
 // scenes; without neighbour masks (maxParInCell > 16) every shape walks
@@ -196,10 +197,10 @@ k_place(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int
 struct WalkShape {
   int threads, dens, force;
 };
-constexpr int kWalkShapes = 9;
+constexpr int kWalkShapes = 11;
 constexpr WalkShape kShapes[kWalkShapes] = {
-    {64, 0, 0}, {128, 0, 0}, {256, 0, 0}, {128, 1, 1}, {128, 2, 2},
-    {256, 2, 2}, {128, 2, 0}, {128, 0, 2}, {64, 2, 2}};
+    {64, 0, 0}, {128, 0, 0}, {256, 0, 0}, {128, 1, 1}, {128, 2, 2}, {256, 2, 2},
+    {128, 2, 0}, {128, 0, 2}, {64, 2, 2}, {128, 2, 3}, {64, 2, 3}};
 constexpr uint32_t kTileDensSlots = 2048, kTileForceSlots = 1536;  // shape 3
 constexpr uint32_t kPairs64 = 512, kPairs128 = 896, kPairs256 = 1792;  // k_density_pairs
 constexpr int kDefaultShape = 4;
@@ -1252,6 +1253,9 @@ void launch_force(SphSystem* s, cudaStream_t st, int b, int v, const StepOpts& o
   else if (kind == 2)
     k_force_fields<kThreads, kMin><<<g, kThreads, 0, st>>>(o.scenes, s->d_poff, s->S, s->N, s->pos[b],
                                                            s->vel[1 - v], s->dp, s->start, s->masks, s->vel[v]);
+  else if (kind == 3 && kThreads <= 128)
+    k_force_coop<kThreads <= 128 ? kThreads : 128><<<g, kThreads, 0, st>>>(
+        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dp, s->start, s->masks, s->vel[v]);
   else
     k_force<true, kThreads, kMin, false><<<g, kThreads, 0, st>>>(
         o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->dp, s->start, s->count,

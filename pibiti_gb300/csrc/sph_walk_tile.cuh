@@ -649,3 +649,152 @@ k_force_fields(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ po
   vel_out[i] = make_float4(__fadd_rn(vi.x, add.x), __fadd_rn(vi.y, add.y), __fadd_rn(vi.z, add.z),
                            __fadd_rn(vi.w, 0.f));
 }
+
+// ---- force, warp-cooperative by rows --------------------------------------------
+// The masked walk one neighbour row (dz, dy) at a time, with the pair terms
+// of the whole warp evaluated together.  For each row:
+//   1. every thread lists its pairs of the row in walk order (candidate
+//      index, owning lane, x field) in the warp's part of shared memory, at
+//      an offset from a warp prefix sum of the threads' pair counts;
+//   2. the warp evaluates the list 32 pairs at a time, each lane taking any
+//      thread's pair (the owner's position, velocity, 1/rho and pressure come
+//      from the warp's particle table), and writes the term to the list's
+//      result slot (zero when r >= h);
+//   3. every thread adds its own results in list order, flushing the cell's
+//      partial sum into its total where the x field changes.
+// Step 2 keeps all lanes busy however unevenly the pairs fall over the
+// threads, which is what limits the one-thread-per-particle walk when cells
+// hold one or two neighbours each; steps 1 and 3 are a few instructions per
+// pair.  The sums are the per-thread walk's, in the same order.  A row whose
+// warp total exceeds kCoopCap pairs is walked one thread per particle.
+constexpr int kCoopCap = 256;
+
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads, 1024 / kThreads)
+k_force_coop(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
+             const float4* __restrict__ pos, const float4* __restrict__ vel,
+             const float2* __restrict__ dp, const uint32_t* __restrict__ start,
+             const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out) {
+  constexpr int kW = kThreads / 32;
+  __shared__ uint2 s_ent[kW][kCoopCap];     // (candidate index, owner lane | field << 8)
+  __shared__ float4 s_res[kW][kCoopCap];    // pair term, w unused
+  __shared__ float4 s_px[kW][32], s_pv[kW][32];  // (x, y, z, 1/rho), (vx, vy, vz, p) per lane
+  const uint32_t i = regrouped_particle<kThreads>(sc, poff, S, N, pos);
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const bool valid = i < N;
+  // a warp whose threads all have no particle leaves together
+  if (!__any_sync(0xffffffffu, valid)) return;
+  const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, valid ? i : N - 1)];
+  const SimParams& p = d.p;
+  float4 xi = make_float4(0.f, 0.f, 0.f, 0.f), vi = xi;
+  float2 dpi = make_float2(0.f, 0.f);
+  if (valid) {
+    xi = __ldg(pos + i);
+    vi = __ldg(vel + i);
+    dpi = __ldg(dp + i);
+  }
+  s_px[w][lane] = make_float4(xi.x, xi.y, xi.z, dpi.x);
+  s_pv[w][lane] = make_float4(vi.x, vi.y, vi.z, dpi.y);
+  const ForceConsts k = force_consts(p);
+  const int3 g0 = grid_pos(p, xi);
+  const int gx = (int)p.gridSize.x, gy = (int)p.gridSize.y, gz = (int)p.gridSize.z;
+  const int cx = min(max(g0.x, 0), gx - 1), cy = min(max(g0.y, 0), gy - 1), cz = min(max(g0.z, 0), gz - 1);
+  float3 F = make_float3(0.f, 0.f, 0.f);
+  auto add = [](float3& a, float x, float y, float z) {
+    a.x = __fadd_rn(a.x, x);
+    a.y = __fadd_rn(a.y, y);
+    a.z = __fadd_rn(a.z, z);
+  };
+  unsigned long long mnext = valid ? masks[i] : 0ull;
+#pragma unroll 1
+  for (int r = 0; r < kRows; ++r) {
+    const unsigned long long m = mnext;
+    if (r + 1 < kRows) mnext = valid ? masks[(size_t)(r + 1) * N + i] : 0ull;
+    // pairs of this row per thread; warp prefix sum and total
+    const uint32_t np = (uint32_t)__popcll((long long)m);
+    uint32_t incl = np;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31), base = incl - np;
+    if (total == 0) continue;
+    const int row = (cz + r / 3 - 1) * (int)p.gridSize_yx + (cy + r % 3 - 1) * gx + cx;  // dx = 0
+    if (total > (uint32_t)kCoopCap) {
+      // a crowded row: one thread per particle, cell field by cell field
+#pragma unroll 1
+      for (int f = 0; f < 3; ++f) {
+        uint32_t bits = (uint32_t)(m >> (16 * (2 - f))) & 0xFFFFu;
+        if (!bits) continue;
+        const uint32_t s0 = __ldg(start + (d.c_off + (uint32_t)(row + f - 1))) + 15u;
+        float3 cell = make_float3(0.f, 0.f, 0.f);
+        do {
+          const int b = 31 - __clz(bits);
+          bits ^= 1u << b;
+          const uint32_t j = s0 - (uint32_t)b;
+          const float4 xj = __ldg(pos + j), vj = __ldg(vel + j);
+          const float2 dpj = __ldg(dp + j);
+          const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
+          const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
+          float3 t;
+          if (force_term(k, vi, dpi.x, dpi.y, vj, dpj.x, dpj.y, rx, ry, rz, dist2, t)) add(cell, t.x, t.y, t.z);
+        } while (bits);
+        add(F, cell.x, cell.y, cell.z);
+      }
+      continue;
+    }
+    // 1. list this thread's pairs of the row, walk order
+    uint32_t q = base;
+#pragma unroll 1
+    for (int f = 0; f < 3; ++f) {
+      uint32_t bits = (uint32_t)(m >> (16 * (2 - f))) & 0xFFFFu;
+      if (!bits) continue;
+      const uint32_t s0 = __ldg(start + (d.c_off + (uint32_t)(row + f - 1))) + 15u;
+      do {
+        const int b = 31 - __clz(bits);
+        bits ^= 1u << b;
+        s_ent[w][q++] = make_uint2(s0 - (uint32_t)b, lane | ((uint32_t)f << 8));
+      } while (bits);
+    }
+    __syncwarp();
+    // 2. all pair terms of the warp's row
+#pragma unroll 1
+    for (uint32_t e = lane; e < total; e += 32) {
+      const uint2 en = s_ent[w][e];
+      const uint32_t j = en.x, own = en.y & 31u;
+      const float4 a = s_px[w][own], b = s_pv[w][own];
+      const float4 xj = __ldg(pos + j), vj = __ldg(vel + j);
+      const float2 dpj = __ldg(dp + j);
+      const float rx = __fsub_rn(a.x, xj.x), ry = __fsub_rn(a.y, xj.y), rz = __fsub_rn(a.z, xj.z);
+      const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
+      float3 t;
+      const bool in = force_term(k, b, a.w, b.w, vj, dpj.x, dpj.y, rx, ry, rz, dist2, t);
+      // r >= h: no term (+0 leaves a partial sum unchanged)
+      s_res[w][e] = in ? make_float4(t.x, t.y, t.z, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncwarp();
+    // 3. this thread's terms in order, the cell sum flushed at each field change
+    if (np) {
+      float3 cell = make_float3(0.f, 0.f, 0.f);
+      uint32_t cur = s_ent[w][base].y >> 8;
+#pragma unroll 1
+      for (uint32_t e = base; e < base + np; ++e) {
+        const uint32_t fld = s_ent[w][e].y >> 8;
+        if (fld != cur) {
+          add(F, cell.x, cell.y, cell.z);
+          cell = make_float3(0.f, 0.f, 0.f);
+          cur = fld;
+        }
+        const float4 t = s_res[w][e];
+        add(cell, t.x, t.y, t.z);
+      }
+      add(F, cell.x, cell.y, cell.z);
+    }
+    __syncwarp();
+  }
+  if (!valid) return;
+  const float3 dv = velocity_increment(p, F, xi, vi);
+  vel_out[i] = make_float4(__fadd_rn(vi.x, dv.x), __fadd_rn(vi.y, dv.y), __fadd_rn(vi.z, dv.z),
+                           __fadd_rn(vi.w, 0.f));
+}

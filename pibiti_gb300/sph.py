@@ -292,13 +292,14 @@ class SPH:
         check(lib().sph_set_persistent(self._h, int(on)))
 
     # by shape (sph_set_walk_shape): threads per block, staged density walk
-    WALK_THREADS = (64, 128, 256, 128, 128, 256, 128, 128, 64)
-    WALK_STAGED = (False, False, False, True, True, True, True, False, True)
+    WALK_THREADS = (64, 128, 256, 128, 128, 256, 128, 128, 64, 128, 64)
+    WALK_STAGED = (False, False, False, True, True, True, True, False, True, True, True)
     # kernel names of the (density, force) walks by shape
     WALK_KERNELS = (("k_density", "k_force"),) * 3 + (("k_density_tile", "k_force_tile"),
                     ("k_density_pairs", "k_force_fields"), ("k_density_pairs", "k_force_fields"),
                     ("k_density_pairs", "k_force"), ("k_density", "k_force_fields"),
-                    ("k_density_pairs", "k_force_fields"))
+                    ("k_density_pairs", "k_force_fields"), ("k_density_pairs", "k_force_coop"),
+                    ("k_density_pairs", "k_force_coop"))
 
     def set_walk_shape(self, shape: int) -> None:
         check(lib().sph_set_walk_shape(self._h, shape))
