@@ -149,12 +149,15 @@ uint32_t sph_scene_offset(const SphSystem* sys, uint32_t scene);
 /* setArray (SPH_Util.cpp:59-71): write `count` float4 records, starting at
    original particle index `start` (indices run over all scenes), from host
    memory (src_on_device = 0) or device memory (1).  Synchronous for host
-   sources. */
+   sources.  A pinned host buffer (one the GPU can address) is read by the
+   GPU directly in one pass; pageable memory goes through a device staging
+   copy. */
 int sph_set_array(SphSystem* sys, uint32_t which, const sph_float4* data, uint32_t start,
                   uint32_t count, int src_on_device);
 /* getArray (SPH_Util.cpp:44-56): all particles in original order, to host
    (dst_on_device = 0, synchronous) or device memory.  `which` is an enum;
-   the reference's inverted bool is not reproduced. */
+   the reference's inverted bool is not reproduced.  A pinned host buffer is
+   written by the GPU directly, as in sph_set_array. */
 int sph_get_array(SphSystem* sys, uint32_t which, sph_float4* out, int dst_on_device);
 
 /* Update (SPH_Update.cpp:12-81) `steps` times: integrate, hash, sort,

@@ -746,6 +746,27 @@ __global__ void k_get_array(const float4* __restrict__ arr, const uint32_t* __re
   if (j < N) dst[id[j]] = arr[j];
 }
 
+// Host buffers the GPU can address (pinned, mapped): the records move
+// between host memory and the state in one pass, in original order on the
+// host side (coalesced over the host link), through the inverse of the
+// stored order, inv[original index] = stored position.
+__global__ void k_inverse(const uint32_t* __restrict__ id, uint32_t* __restrict__ inv, uint32_t N) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < N) inv[id[j]] = j;
+}
+
+__global__ void k_set_array_host(float4* __restrict__ arr, const uint32_t* __restrict__ inv,
+                                 const float4* __restrict__ src, uint32_t start, uint32_t cnt) {
+  const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o < cnt) arr[inv[start + o]] = src[o];
+}
+
+__global__ void k_get_array_host(const float4* __restrict__ arr, const uint32_t* __restrict__ inv,
+                                 float4* __restrict__ dst, uint32_t N) {
+  const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o < N) dst[o] = arr[inv[o]];
+}
+
 __global__ void k_sorted_hash(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff,
                               int S, uint32_t N, const float4* __restrict__ pos,
                               const uint32_t* __restrict__ id, uint2* __restrict__ out) {
@@ -1102,6 +1123,7 @@ struct SphSystem {
   uint32_t* flags = nullptr;
   double* stats = nullptr;
   float4* staging = nullptr;
+  uint32_t* inv = nullptr;           // stored position of each original index (host transfers)
   int cp = 0;  // pos/id buffer holding the state
   int cv = 0;  // vel buffer holding the state
   bool stepped = false;
@@ -1377,7 +1399,7 @@ void free_all(SphSystem* s) {
   drop_graphs(s);
   void* bufs[] = {s->d_scenes, s->d_poff, s->d_coff, s->pos[0], s->pos[1], s->vel[0], s->vel[1],
                   s->id[0], s->id[1], s->key, s->rank, s->slot, s->dest, s->count, s->start, s->scan_tmp,
-                  s->dens, s->pres, s->dp, s->masks, s->flags, s->stats, s->staging, s->d_coarse,
+                  s->dens, s->pres, s->dp, s->masks, s->flags, s->stats, s->staging, s->inv, s->d_coarse,
                   s->mlp_img, s->mlp_aux, s->feat, s->mlp_y, s->bk_vel, s->vstart, s->hist, s->ptsum, s->pbar,
                   s->big_list, s->sort_counters, s->sort_list, s->sort_scratch};
   for (void* p : bufs)
@@ -1497,6 +1519,24 @@ int ensure_staging(SphSystem* s) {
   return SPH_OK;
 }
 
+// The device address of a host buffer the GPU can reach (pinned and mapped
+// into the address space), or null for pageable memory.
+const void* device_view(const void* host) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// inv from the stored order of the current state.
+int refresh_inverse(SphSystem* s) {
+  if (!s->inv) SPH_TRY(dalloc(&s->inv, s->N, "inverse order"));
+  k_inverse<<<grid_for(s->N, kBlock), kBlock, 0, s->stream>>>(s->id[s->cp], s->inv, s->N);
+  return cuda_check(cudaGetLastError(), "inverse order");
+}
+
 }  // namespace
 
 extern "C" {
@@ -1563,6 +1603,16 @@ int sph_set_array(SphSystem* s, uint32_t which, const sph_float4* data, uint32_t
   s->lr_refs = 0;  // the learned step's density history no longer applies
   if ((uint64_t)start + count > s->N) return fail(SPH_ERR_ARG, "set_array: range beyond %u particles", s->N);
   if (count == 0) return SPH_OK;
+  if (!src_on_device) {
+    if (const void* dv = device_view(data)) {  // pinned: one pass over the host link
+      SPH_TRY(refresh_inverse(s));
+      float4* arr = which == SPH_ARRAY_POS ? s->pos[s->cp] : s->vel[s->cv];
+      k_set_array_host<<<grid_for(count, kBlock), kBlock, 0, s->stream>>>(arr, s->inv, (const float4*)dv,
+                                                                          start, count);
+      SPH_CUDA(cudaGetLastError(), "set_array kernel");
+      return cuda_check(cudaStreamSynchronize(s->stream), "set_array sync");
+    }
+  }
   SPH_TRY(ensure_staging(s));
   SPH_CUDA(cudaMemcpyAsync(s->staging, data, sizeof(float4) * count,
                            src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s->stream),
@@ -1580,6 +1630,12 @@ int sph_get_array(SphSystem* s, uint32_t which, sph_float4* out, int dst_on_devi
   const float4* arr = which == SPH_ARRAY_POS ? s->pos[s->cp] : s->vel[s->cv];
   float4* dst = (float4*)out;
   if (!dst_on_device) {
+    if (const void* dv = device_view(out)) {  // pinned: one pass over the host link
+      SPH_TRY(refresh_inverse(s));
+      k_get_array_host<<<grid_for(s->N, kBlock), kBlock, 0, s->stream>>>(arr, s->inv, (float4*)dv, s->N);
+      SPH_CUDA(cudaGetLastError(), "get_array kernel");
+      return cuda_check(cudaStreamSynchronize(s->stream), "get_array sync");
+    }
     SPH_TRY(ensure_staging(s));
     dst = s->staging;
   }
