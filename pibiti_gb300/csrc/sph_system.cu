@@ -1124,6 +1124,7 @@ struct SphSystem {
   double* stats = nullptr;
   float4* staging = nullptr;
   uint32_t* inv = nullptr;           // stored position of each original index (host transfers)
+  bool inv_ok = false;               // inv matches the current order (cleared by every step)
   int cp = 0;  // pos/id buffer holding the state
   int cv = 0;  // vel buffer holding the state
   bool stepped = false;
@@ -1372,6 +1373,7 @@ int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr,
   SPH_CUDA(cudaGetLastError(), "step kernels");
   s->cp = b;
   s->stepped = true;
+  s->inv_ok = false;
   return SPH_OK;
 }
 
@@ -1532,9 +1534,12 @@ const void* device_view(const void* host) {
 
 // inv from the stored order of the current state.
 int refresh_inverse(SphSystem* s) {
+  if (s->inv_ok) return SPH_OK;
   if (!s->inv) SPH_TRY(dalloc(&s->inv, s->N, "inverse order"));
   k_inverse<<<grid_for(s->N, kBlock), kBlock, 0, s->stream>>>(s->id[s->cp], s->inv, s->N);
-  return cuda_check(cudaGetLastError(), "inverse order");
+  SPH_CUDA(cudaGetLastError(), "inverse order");
+  s->inv_ok = true;
+  return SPH_OK;
 }
 
 }  // namespace
@@ -1733,6 +1738,7 @@ int sph_step(SphSystem* s, uint32_t steps) {
     if (steps) {
       SPH_TRY(persistent_steps(s, steps));
       s->stepped = true;
+      s->inv_ok = false;
     }
     return SPH_OK;
   }
@@ -1744,7 +1750,10 @@ int sph_step(SphSystem* s, uint32_t steps) {
       SPH_CUDA(cudaGraphLaunch(s->graph[s->cp], s->stream), "step graph launch");
   }
   for (; done < steps; ++done) SPH_TRY(enqueue_step(s, s->stream));
-  if (steps) s->stepped = true;
+  if (steps) {
+    s->stepped = true;
+    s->inv_ok = false;
+  }
   return SPH_OK;
 }
 
@@ -1830,6 +1839,7 @@ int sph_autotune(SphSystem* s, uint32_t trial_steps, float* ms_per_step, uint32_
   if (rc == SPH_OK) rc = cuda_check(cudaStreamSynchronize(s->stream), "autotune: restore");
   s->walk_shape = rc == SPH_OK ? best_shape : shape0;
   s->stepped = stepped0 || rc == SPH_OK;
+  s->inv_ok = false;
   drop_graphs(s);
   if (chosen) *chosen = (uint32_t)s->walk_shape;
   if (e0) cudaEventDestroy(e0);
@@ -1997,6 +2007,7 @@ int sph_learned_step(SphSystem* s, uint32_t coarse_steps, uint32_t substeps, flo
       SPH_CUDA(cudaGraphLaunch(s->lgraph[cp0], s->stream), "learned step graph launch");
       s->cp = 1 - cp0;
       s->stepped = true;
+      s->inv_ok = false;
     } else {
       SPH_TRY(enqueue_coarse(s->stream));
     }
