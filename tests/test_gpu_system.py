@@ -111,6 +111,41 @@ def test_drift_against_fp64_trajectory(cuda):
     assert p.restDensity < rho32[-1] < 4 * p.restDensity
 
 
+# Measured: kinetic energy 1.8e-6 and 5.7e-6, mean density 4.9e-6 and 2.5e-6
+# (relative, at steps 100 and 200).
+DRIFT_1M_STEPS = 200
+DRIFT_1M_KE, DRIFT_1M_RHO = 1e-4, 1e-4          # relative, at steps 100 and 200
+
+
+def test_drift_against_fp64_trajectory_1m(cuda):
+    """200 steps of the 1,048,576-particle double dam break (the columns
+    falling, before they meet): the GPU's kinetic energy and mean density
+    against the double-precision trajectory's, every 100 steps."""
+    w = configs.dambreak_double()
+    p = Scene.parse(w.xml).params
+    ke32, rho32 = [], []
+    with system_from(p, w.pos, w.vel) as s:
+        for _ in range(DRIFT_1M_STEPS // 100):
+            s.update(100)
+            st = s.stats()[0]
+            assert st[3] == 0
+            ke32.append(st[0])
+            rho32.append(st[1])
+    ke64, rho64 = [], []
+    pos, vel = w.pos, w.vel
+    m = float(p.particleMass)
+    for _ in range(DRIFT_1M_STEPS // 100):
+        pos, vel, md = oracle.step_fp64(p, pos, vel, steps=100, with_density=True)
+        ke64.append(0.5 * m * float((vel[:, :3] ** 2).sum()))
+        rho64.append(md)
+    ke32, rho32, ke64, rho64 = map(np.asarray, (ke32, rho32, ke64, rho64))
+    dke = np.abs(ke32 - ke64) / ke64
+    drho = np.abs(rho32 - rho64) / rho64
+    print("1M drift vs FP64: KE", dke, "mean density", drho)
+    assert dke.max() <= DRIFT_1M_KE, dke
+    assert drho.max() <= DRIFT_1M_RHO, drho
+
+
 def test_stats_reductions_at_1m(cuda):
     """The GPU's kinetic-energy and mean-density reductions after 200 steps
     of the 1,048,576-particle double dam break, against double-precision sums
