@@ -295,6 +295,21 @@ int sph_mlp_forward_tc_withheld(const void* packed, const uint16_t* x, uint32_t 
    (both FP32, zeroed by the caller). */
 int sph_mlp_train_pass(const void* packed, const uint16_t* x, const float* target, uint32_t n,
                        float* grad, float* loss, void* stream);
+/* The same training pass on the 5th-generation tensor cores: forward,
+   backward and weight-gradient products as tcgen05.mma with the
+   accumulators in tensor memory (the weight gradients accumulate there over
+   all of a thread block's 128-sample tiles), the same BF16 roundings as
+   sph_mlp_train_pass; only the FP32 summation order differs.  x must be
+   16-byte aligned.  Its waits for the tensor cores are bounded: a thread
+   block whose wait runs out adds NaN to *loss, adds nothing to grad and sets
+   bit 1 of the status word of sph_mlp_status. */
+int sph_mlp_train_pass_tc(const void* packed, const uint16_t* x, const float* target, uint32_t n,
+                          float* grad, float* loss, void* stream);
+/* Test hook for the timeout path of sph_mlp_train_pass_tc: the tensor-core
+   work withheld and each wait bounded at 1024 polls; *loss becomes NaN,
+   grad is untouched, status bit 1 is set, and the tensor memory is freed. */
+int sph_mlp_train_pass_tc_withheld(const void* packed, const uint16_t* x, const float* target,
+                                   uint32_t n, float* grad, float* loss, void* stream);
 /* Adam step `step` (1-based) on the FP32 parameters with moments m, v. */
 int sph_mlp_adam(float* params, float* m, float* v, const float* grad, float lr, float beta1,
                  float beta2, float eps, uint32_t step, void* stream);

@@ -117,6 +117,8 @@ SIGNATURES = {
     "sph_mlp_forward_tc_withheld": [vp, vp, u32, vp, vp],
     "sph_mlp_status": [P(u32)],
     "sph_mlp_train_pass": [vp, vp, vp, u32, vp, vp, vp],
+    "sph_mlp_train_pass_tc": [vp, vp, vp, u32, vp, vp, vp],
+    "sph_mlp_train_pass_tc_withheld": [vp, vp, vp, u32, vp, vp, vp],
     "sph_mlp_adam": [vp, vp, vp, vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                      ctypes.c_float, u32, vp],
     "sph_learned_set_model": [vp, vp, vp, vp],

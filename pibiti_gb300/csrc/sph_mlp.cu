@@ -1,9 +1,9 @@
 // sph_mlp.cu -- the per-particle MLP corrector (16 -> 64 -> 64 -> 3, tanh)
-// on the tensor cores: BF16 operands, FP32 accumulation.  Training (forward
-// and backward) and one forward pass use mma.sync m16n8k16 (one warp = 16
-// particles per tile); the forward pass the learned step runs is a tcgen05
-// kernel with TMEM accumulators (k_forward_tc, at the end), bit-identical to
-// the mma.sync one.
+// on the tensor cores: BF16 operands, FP32 accumulation.  Two forms of each
+// pass: mma.sync m16n8k16 (one warp = 16 particles per tile: k_forward,
+// k_train) and tcgen05 kernels with TMEM accumulators (k_forward_tc, which
+// the learned step runs, bit-identical to k_forward; k_train_tc, which
+// training runs, equal to k_train up to FP32 summation order).
 //
 // Parameters are kept in FP32 (training master copy) in one vector:
 //   W1[16][64] b1[64] W2[64][64] b2[64] W3[64][3] b3[3]   (5443 floats)
@@ -750,6 +750,333 @@ __global__ void __launch_bounds__(128, tcg::kBlocksPerSm) k_forward_tc(const uin
   if (w == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
 }
+
+// ---- tcgen05 training --------------------------------------------------------
+// One training pass (sph_mlp_train_pass_tc) on the 5th-generation tensor
+// cores: one CTA of 128 threads per 128-sample tile (grid-stride over
+// tiles), thread t owning sample t of the tile.  Per tile, every product
+// is a tcgen05.mma chain with BF16 operands in shared memory and FP32
+// accumulators in tensor memory:
+//   forward   Z1 = X W1 + b1, Z2 = H1 W2 + b2, Y = H2 W3 + b3 (as k_forward_tc)
+//   backward  dH2 = dY W3^T, dH1 = dZ2 W2^T   (dZ = dH (1 - H^2), per thread)
+//   gradients G2 = dZ2^T [H1 | 1], G3 = dY^T [H2 | 1], G1 = dZ1^T [X | 1]
+// The weight-gradient products contract over the tile's samples.  They read
+// the activations and gradients where the forward and backward products
+// left them (rows = samples): as operands whose M or N dimension is the
+// contiguous one (MN-major, transpose bits 15 and 16 of the instruction
+// descriptor; leading byte offset = the stride between core matrices along
+// K, the samples, and stride byte offset = the stride along M or N), so no
+// transposed copy is made.  A ones column appended to H1, H2 and X puts the
+// bias gradients (column sums of dZ2, dY, dZ1) in column 64, 64 and 16 of
+// G2, G3 and G1.  The M dimension of every product is 128: G2 and G1 have
+// 64 real rows and G3 3; the other rows read whatever lies beyond the
+// operand in shared memory and are never used (row r of a product depends
+// on row r of A alone).  The three gradient accumulators stay in tensor
+// memory across all tiles of the CTA (256 columns: scratch 0-63, G2 64-143,
+// G3 144-223, G1 224-255) and are added to `grad` once at the end, one
+// atomicAdd per parameter and CTA.  BF16 roundings are the mma.sync pass's
+// (k_train): X, H1, H2, dY, dZ2, dZ1 and the weights.  Every wait is
+// bounded; a CTA whose wait runs out sets status bit 1, adds NaN to *loss
+// and adds nothing to `grad`.
+namespace tct {
+using namespace tcg;
+// shared memory (bytes); the operands whose garbage rows read past their
+// end (dZ2, dZ1: 1 KB; dY: 1.8 KB) are followed by other buffers
+constexpr uint32_t tDZ2 = 0;        // 128 x 64, 8 K-cores per row group
+constexpr uint32_t tDZ1 = 16384;    // 128 x 64
+constexpr uint32_t tDY = 32768;     // 128 x 16 (outputs 0..2, then zeros)
+constexpr uint32_t tX = 36864;      // 128 x 32: inputs 0..15, a one, zeros
+constexpr uint32_t tH1 = 45056;     // 128 x 80: hidden 0..63, a one, zeros
+constexpr uint32_t tH2 = 65536;     // 128 x 80
+constexpr uint32_t tW1 = 86016;     // W1^T 64 x 16
+constexpr uint32_t tW2 = 88064;     // W2^T 64 x 64
+constexpr uint32_t tW3 = 96256;     // W3^T 16 x 64 (rows 3..15 zero)
+constexpr uint32_t tW3r = 98304;    // W3 64 x 16 (in-major; columns 3..15 zero)
+constexpr uint32_t tW2r = 100352;   // W2 64 x 64 (in-major)
+constexpr uint32_t tBias = 108544;  // b1[64] b2[64] b3[4]
+constexpr uint32_t tBar = 109088;
+constexpr uint32_t tTmem = 109096;
+constexpr uint32_t kTrSmem = 109184;
+constexpr uint32_t kTrCols = 256;
+constexpr uint32_t cG2 = 64, cG3 = 144, cG1 = 224;  // TMEM columns of the gradients
+constexpr uint32_t kTrBlocks = 2;
+static_assert(kTrBlocks * kTrCols <= 512, "TMEM columns of the resident CTAs");
+static_assert(kTrBlocks * (kTrSmem + 1024) <= 233472, "shared memory of the resident CTAs");
+static_assert(tDZ2 + 15 * 128 + 15 * 1024 + 128 <= tDY, "dZ2 garbage rows stay in shared memory");
+static_assert(tDZ1 + 15 * 128 + 15 * 1024 + 128 <= tX, "dZ1 garbage rows stay in shared memory");
+static_assert(tDY + 15 * 128 + 15 * 256 + 128 <= kTrSmem, "dY garbage rows stay in shared memory");
+static_assert(tTmem + 4 <= kTrSmem, "layout");
+constexpr uint32_t kMN = (1u << 15) | (1u << 16);  // A and B MN-major
+
+__device__ __forceinline__ void ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+               : "r"(taddr)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+// 64 bias values (b1 or b2) into this thread's scratch columns 0..63.
+__device__ __forceinline__ void seed64(uint32_t lane_base, const float* b) {
+#pragma unroll 1
+  for (int q = 0; q < 4; ++q) st16(lane_base + 16u * q, b + 16 * q);
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+// tanh of this thread's 64 scratch columns as BF16 into row t of an
+// activation buffer of 10 K-cores per row group.
+__device__ __forceinline__ void activate10(uint32_t lane_base, uint8_t* hbuf, uint32_t t) {
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    float v[32];
+    ld32(lane_base + 32u * half, v);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t pk[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) pk[j] = tanh_pack2(v[8 * q + 2 * j], v[8 * q + 2 * j + 1]);
+      *reinterpret_cast<uint4*>(hbuf + core_off(t, 32u * half + 8u * q, 10)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+  }
+}
+// dZ = dH (1 - h^2) for this thread's row: dH from scratch columns 0..63,
+// h (BF16) from row t of `hbuf` (10 K-cores), dZ as BF16 into row t of
+// `zbuf` (8 K-cores).
+__device__ __forceinline__ void grad_act(uint32_t lane_base, const uint8_t* hbuf, uint8_t* zbuf, uint32_t t) {
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    float v[32];
+    ld32(lane_base + 32u * half, v);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint32_t c0 = 32u * half + 8u * q;
+      const uint4 h = *reinterpret_cast<const uint4*>(hbuf + core_off(t, c0, 10));
+      const uint32_t hw[4] = {h.x, h.y, h.z, h.w};
+      uint32_t pk[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float h0 = lo_of(hw[j]), h1 = hi_of(hw[j]);
+        pk[j] = pack2(v[8 * q + 2 * j] * (1.f - h0 * h0), v[8 * q + 2 * j + 1] * (1.f - h1 * h1));
+      }
+      *reinterpret_cast<uint4*>(zbuf + core_off(t, c0, 8)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    }
+  }
+}
+}  // namespace tct
+
+__global__ void __launch_bounds__(128, tct::kTrBlocks) k_train_tc(const uint16_t* __restrict__ img,
+                                                                     const uint16_t* __restrict__ x,
+                                                                     const float* __restrict__ target,
+                                                                     uint32_t n, float inv_count,
+                                                                     float* __restrict__ grad,
+                                                                     float* __restrict__ loss,
+                                                                     uint32_t spins, bool withhold) {
+  using namespace tct;
+  extern __shared__ __align__(128) uint8_t sm[];
+  const uint32_t t = threadIdx.x, w = t >> 5;
+  const uint32_t sb = (uint32_t)__cvta_generic_to_shared(sm);
+  const uint32_t tiles = (n + 127) / 128;
+  // weights (K-major core-matrix layout) and biases, once per CTA
+  {
+    const uint32_t o = t >> 1, c = t & 1u;  // W1^T, W3 in-major: 64 rows x 2 chunks
+    *reinterpret_cast<uint4*>(sm + tW1 + core_off(o, 8 * c, 2)) =
+        *reinterpret_cast<const uint4*>(img + oWT1 + o * S1 + 8 * c);
+    *reinterpret_cast<uint4*>(sm + tW3r + core_off(o, 8 * c, 2)) =
+        *reinterpret_cast<const uint4*>(img + mlp::oW3r + o * S3r + 8 * c);
+  }
+  for (uint32_t e = t; e < 64 * 8; e += 128) {  // W2^T and W2: 64 rows x 8 chunks
+    const uint32_t o = e >> 3, c = e & 7u;
+    *reinterpret_cast<uint4*>(sm + tW2 + core_off(o, 8 * c, 8)) =
+        *reinterpret_cast<const uint4*>(img + oWT2 + o * S2 + 8 * c);
+    *reinterpret_cast<uint4*>(sm + tW2r + core_off(o, 8 * c, 8)) =
+        *reinterpret_cast<const uint4*>(img + mlp::oW2r + o * S2 + 8 * c);
+  }
+  {  // W3^T: rows 0..7 from the image (3..7 are zero there), rows 8..15 zero
+    const uint32_t o = t >> 3, c = t & 7u;  // 16 rows x 8 chunks
+    *reinterpret_cast<uint4*>(sm + tW3 + core_off(o, 8 * c, 8)) =
+        o < 8 ? *reinterpret_cast<const uint4*>(img + oWT3 + o * S2 + 8 * c) : make_uint4(0, 0, 0, 0);
+  }
+  const float* bimg = reinterpret_cast<const float*>(img + kHalves);  // b1 b2 b3
+  float* sbias = reinterpret_cast<float*>(sm + tBias);
+  sbias[t] = bimg[t];
+  if (t < 4) sbias[128 + t] = t < OUT ? bimg[2 * HID + t] : 0.f;
+  // the constant columns: X 16..31 = (1, 0, ...), H1 and H2 64..79 = (1, 0, ...)
+  const uint4 one = make_uint4(0x3F80u, 0u, 0u, 0u), zero = make_uint4(0u, 0u, 0u, 0u);
+  *reinterpret_cast<uint4*>(sm + tX + core_off(t, 16, 4)) = one;
+  *reinterpret_cast<uint4*>(sm + tX + core_off(t, 24, 4)) = zero;
+  *reinterpret_cast<uint4*>(sm + tH1 + core_off(t, 64, 10)) = one;
+  *reinterpret_cast<uint4*>(sm + tH1 + core_off(t, 72, 10)) = zero;
+  *reinterpret_cast<uint4*>(sm + tH2 + core_off(t, 64, 10)) = one;
+  *reinterpret_cast<uint4*>(sm + tH2 + core_off(t, 72, 10)) = zero;
+  if (t == 0) mbar_init(sb + tBar);
+  if (w == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sb + tTmem),
+                 "r"(kTrCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  sync_for_mma();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + tTmem);
+  const uint32_t lane_base = tmem + ((32u * w) << 16);
+  uint32_t phase = 0;
+  bool ok = true, pending = false, started = false;
+  auto run = [&](auto issue) {
+    if (t == 0 && !withhold) {
+      issue();
+      commit(sb + tBar);
+    }
+    pending = !withhold;
+    ok = __syncthreads_and(mbar_wait(sb + tBar, phase, spins));
+    if (!ok) return false;
+    pending = false;
+    phase ^= 1u;
+    fence_after();
+    return true;
+  };
+  float lsum = 0.f;
+  for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const uint32_t row = tile * 128 + t;
+    {  // X row t (zeros past n: such rows get dY = 0 and add nothing)
+      uint4 c0 = zero, c1 = zero;
+      if (row < n) {
+        const uint4* src = reinterpret_cast<const uint4*>(x + (size_t)row * IN);
+        c0 = src[0];
+        c1 = src[1];
+      }
+      *reinterpret_cast<uint4*>(sm + tX + core_off(t, 0, 4)) = c0;
+      *reinterpret_cast<uint4*>(sm + tX + core_off(t, 8, 4)) = c1;
+    }
+    seed64(lane_base, sbias);
+    sync_for_mma();
+    if (!run([&] { umma(tmem, sdesc(sb + tX, 128, 512), sdesc(sb + tW1, 128, 256), idesc(128, 64), 1u); }))
+      break;
+    activate10(lane_base, sm + tH1, t);
+    seed64(lane_base, sbias + 64);
+    sync_for_mma();
+    if (!run([&] {
+          const uint64_t a = sdesc(sb + tH1, 128, 1280), b = sdesc(sb + tW2, 128, 1024);
+#pragma unroll 1
+          for (uint32_t kk = 0; kk < 4; ++kk) umma(tmem, a + 16u * kk, b + 16u * kk, idesc(128, 64), 1u);
+        }))
+      break;
+    activate10(lane_base, sm + tH2, t);
+    {
+      const float4 b3 = *reinterpret_cast<const float4*>(sbias + 128);
+      asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(lane_base),
+                   "r"(__float_as_uint(b3.x)), "r"(__float_as_uint(b3.y)), "r"(__float_as_uint(b3.z)),
+                   "r"(__float_as_uint(b3.w))
+                   : "memory");
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    }
+    sync_for_mma();
+    if (!run([&] {
+          const uint64_t a = sdesc(sb + tH2, 128, 1280), b = sdesc(sb + tW3, 128, 1024);
+#pragma unroll 1
+          for (uint32_t kk = 0; kk < 4; ++kk) umma(tmem, a + 16u * kk, b + 16u * kk, idesc(128, 16), 1u);
+        }))
+      break;
+    {  // dL/dy = 2 (y - target) / count for the 3 outputs, BF16 into dY row t
+      float y[4];
+      ld4(lane_base, y);
+      float d[3] = {0.f, 0.f, 0.f};
+      if (row < n) {
+#pragma unroll
+        for (int c = 0; c < OUT; ++c) {
+          const float e = y[c] - target[(size_t)row * OUT + c];
+          lsum = fmaf(e, e, lsum);
+          d[c] = 2.f * e * inv_count;
+        }
+      }
+      *reinterpret_cast<uint4*>(sm + tDY + core_off(t, 0, 2)) = make_uint4(pack2(d[0], d[1]), pack2(d[2], 0.f), 0u, 0u);
+      *reinterpret_cast<uint4*>(sm + tDY + core_off(t, 8, 2)) = zero;
+    }
+    sync_for_mma();
+    if (!run([&] { umma(tmem, sdesc(sb + tDY, 128, 256), sdesc(sb + tW3r, 128, 256), idesc(128, 64), 0u); }))
+      break;
+    grad_act(lane_base, sm + tH2, sm + tDZ2, t);  // dZ2
+    sync_for_mma();
+    if (!run([&] {
+          {  // dH1 = dZ2 W2^T
+            const uint64_t a = sdesc(sb + tDZ2, 128, 1024), b = sdesc(sb + tW2r, 128, 1024);
+#pragma unroll 1
+            for (uint32_t kk = 0; kk < 4; ++kk) umma(tmem, a + 16u * kk, b + 16u * kk, idesc(128, 64), kk > 0);
+          }
+          // G2 += dZ2^T [H1 | 1], G3 += dY^T [H2 | 1]: K = the tile's 128 samples
+          const uint64_t a2 = sdesc(sb + tDZ2, 1024, 128), b2 = sdesc(sb + tH1, 1280, 128);
+          const uint64_t a3 = sdesc(sb + tDY, 256, 128), b3 = sdesc(sb + tH2, 1280, 128);
+#pragma unroll 1
+          for (uint32_t kk = 0; kk < 8; ++kk) {
+            const uint32_t acc = started || kk > 0;
+            umma(tmem + cG2, a2 + 128u * kk, b2 + 160u * kk, idesc(128, 80) | kMN, acc);
+            umma(tmem + cG3, a3 + 32u * kk, b3 + 160u * kk, idesc(128, 80) | kMN, acc);
+          }
+        }))
+      break;
+    grad_act(lane_base, sm + tH1, sm + tDZ1, t);  // dZ1
+    sync_for_mma();
+    if (!run([&] {  // G1 += dZ1^T [X | 1]
+          const uint64_t a = sdesc(sb + tDZ1, 1024, 128), b = sdesc(sb + tX, 512, 128);
+#pragma unroll 1
+          for (uint32_t kk = 0; kk < 8; ++kk)
+            umma(tmem + cG1, a + 128u * kk, b + 64u * kk, idesc(128, 32) | kMN, started || kk > 0);
+        }))
+      break;
+    started = true;
+  }
+  if (ok && started) {
+    // G2 row o = t (t < 64): dW2[i][o] in columns i, db2[o] in column 64;
+    // G1 row i = t: dW1[j][i] in columns j, db1[i] in column 16;
+    // G3 row c = t (t < 3): dW3[i][c] in columns i, db3[c] in column 64.
+    // tcgen05.ld is warp-wide, so warps 0 and 1 (rows 0..63) read them.
+    if (w < 2) {
+#pragma unroll 1
+      for (int half = 0; half < 2; ++half) {
+        float v[32];
+        ld32(lane_base + cG2 + 32u * half, v);
+#pragma unroll 8
+        for (int k = 0; k < 32; ++k) atomicAdd(grad + pW2 + (32 * half + k) * HID + t, v[k]);
+      }
+      float v[16];
+      ld16(lane_base + cG2 + 64u, v);
+      atomicAdd(grad + pB2 + t, v[0]);
+      ld16(lane_base + cG1, v);
+#pragma unroll
+      for (int j = 0; j < IN; ++j) atomicAdd(grad + pW1 + j * HID + t, v[j]);
+      float vb[16];
+      ld16(lane_base + cG1 + 16u, vb);
+      atomicAdd(grad + pB1 + t, vb[0]);
+    }
+    if (w == 0) {
+#pragma unroll 1
+      for (int half = 0; half < 2; ++half) {
+        float v[32];
+        ld32(lane_base + cG3 + 32u * half, v);
+        if (t < OUT)
+#pragma unroll 8
+          for (int k = 0; k < 32; ++k) atomicAdd(grad + pW3 + (32 * half + k) * OUT + t, v[k]);
+      }
+      float v[16];
+      ld16(lane_base + cG3 + 64u, v);
+      if (t < OUT) atomicAdd(grad + pB3 + t, v[0]);
+    }
+  }
+  if (!ok) {
+    if (t == 0) {
+      atomicOr(&g_tc_status, 2u);
+      atomicAdd(loss, __int_as_float(0x7fc00000));
+    }
+    if (pending) __syncthreads_and(mbar_wait(sb + tBar, phase, spins));  // the MMAs still in flight
+  } else {
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if ((t & 31u) == 0) atomicAdd(loss, lsum * inv_count);
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (w == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTrCols) : "memory");
+}
 }  // namespace
 
 extern "C" {
@@ -811,6 +1138,34 @@ int sph_mlp_train_pass(const void* packed, const uint16_t* x, const float* targe
   k_train<<<blocks, kTrainThreads, kTrainSmem, (cudaStream_t)stream>>>(
       (const uint16_t*)packed, x, target, n, 1.0f / (3.0f * (float)n), grad, loss);
   return cuda_check(cudaGetLastError(), "mlp_train");
+}
+
+static int train_tc(const void* packed, const uint16_t* x, const float* target, uint32_t n, float* grad,
+                    float* loss, void* stream, uint32_t spins, bool withhold, const char* who) {
+  if (!packed || !x || !target || !grad || !loss) return fail(SPH_ERR_ARG, "%s: null pointer", who);
+  if ((uintptr_t)x & 15u) return fail(SPH_ERR_ARG, "%s: features not 16-byte aligned", who);
+  if (n == 0) return SPH_OK;
+  static int attr = -1;
+  if (attr < 0)
+    attr = cuda_check(cudaFuncSetAttribute(k_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)tct::kTrSmem),
+                      "mlp_train_tc: shared memory limit");
+  SPH_TRY(attr);
+  const uint32_t tiles = (n + 127) / 128;
+  const uint32_t blocks = (uint32_t)min((long long)tiles, (long long)sm_count() * tct::kTrBlocks);
+  k_train_tc<<<blocks, 128, tct::kTrSmem, (cudaStream_t)stream>>>(
+      (const uint16_t*)packed, x, target, n, 1.0f / (3.0f * (float)n), grad, loss, spins, withhold);
+  return cuda_check(cudaGetLastError(), who);
+}
+
+int sph_mlp_train_pass_tc(const void* packed, const uint16_t* x, const float* target, uint32_t n,
+                          float* grad, float* loss, void* stream) {
+  return train_tc(packed, x, target, n, grad, loss, stream, tcg::kTcSpins, false, "mlp_train_tc");
+}
+
+int sph_mlp_train_pass_tc_withheld(const void* packed, const uint16_t* x, const float* target, uint32_t n,
+                                   float* grad, float* loss, void* stream) {
+  return train_tc(packed, x, target, n, grad, loss, stream, 1024u, true, "mlp_train_tc_withheld");
 }
 
 int sph_mlp_adam(float* params, float* m, float* v, const float* grad, float lr, float beta1,

@@ -13,7 +13,7 @@ of the fine-dt run, one featured coarse step and SUBSTEPS fine steps give one
 (features, target) pair per particle.  Then, for a few rounds, the states the
 learned integrator itself visits are labelled the same way and added (the
 network then learns to correct the states its own errors lead to).  Training runs the project's own
-forward/backward kernels (sph_mlp_train_pass) with Adam (sph_mlp_adam).
+forward/backward kernels (sph_mlp_train_pass_tc, on tcgen05) with Adam (sph_mlp_adam).
 Device buffers are torch tensors passed by pointer.
 """
 from __future__ import annotations
@@ -228,7 +228,7 @@ def train(feats, targets, epochs: int = 6, batch: int = 65536, lr: float = 2e-3,
             xb, tb = x[idx].contiguous(), t[idx].contiguous()
             grad.zero_()
             loss.zero_()
-            _lib.check(L.sph_mlp_train_pass(_p(img), _p(xb), _p(tb), batch, _p(grad), _p(loss), None))
+            _lib.check(L.sph_mlp_train_pass_tc(_p(img), _p(xb), _p(tb), batch, _p(grad), _p(loss), None))
             step += 1
             _lib.check(L.sph_mlp_adam(_p(prm), _p(m), _p(v), _p(grad), lr_ep, 0.9, 0.999, 1e-8,
                                       step, None))
