@@ -288,6 +288,29 @@ __device__ __forceinline__ bool force_term(const ForceConsts& k, float4 vi, floa
   return r < k.h;
 }
 
+// force_term with the x and y components as FP32 pairs (sm_100+ packed
+// instructions; each half rounds as the scalar _rn operation): vj - vi as
+// fma(vi, -1, vj), which is the IEEE difference with the same signed zeros,
+// and the force's x and y in one multiply, fma and multiply each.  Same
+// result bits as force_term.
+__device__ __forceinline__ bool force_term_xy(const ForceConsts& k, float2 vi_xy, float vi_z, float inv_di,
+                                              float pi, float4 vj, float inv_dj, float pj, float2 r_xy,
+                                              float rz, float dist2, float2& f_xy, float& f_z) {
+  const float dd = __fmul_rn(inv_di, inv_dj);
+  const float d12 = fminf(k.minDens, dd);
+  const float2 v_xy = __ffma2_rn(vi_xy, make_float2(-1.f, -1.f), make_float2(vj.x, vj.y));
+  const float vz = __fsub_rn(vj.z, vi_z);
+  const float r = fmaxf(k.minDist, __fsqrt_rn(dist2));
+  const float c = __fsub_rn(k.h, r);
+  const float pterm = __fdiv_rn(__fmul_rn(__fmul_rn(c, k.spiky), __fadd_rn(pi, pj)), r);
+  const float s = __fmul_rn(c, d12);
+  const float2 t = __ffma2_rn(make_float2(pterm, pterm), r_xy,
+                              __fmul2_rn(make_float2(k.vterm, k.vterm), v_xy));
+  f_xy = __fmul2_rn(t, make_float2(s, s));
+  f_z = __fmul_rn(__fmaf_rn(pterm, rz, __fmul_rn(k.vterm, vz)), s);
+  return r < k.h;
+}
+
 // The part of force_pair after the squared distance; the fused walk calls it
 // only for candidates not excluded by ForceConsts::h2_out (and for NaN).
 __device__ __forceinline__ void force_pair_near(const ForceConsts& k, float4 vi, float inv_di,

@@ -606,7 +606,10 @@ k_force_fields(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ po
   const int3 g0 = grid_pos(p, xi);
   const int gx = (int)p.gridSize.x, gy = (int)p.gridSize.y, gz = (int)p.gridSize.z;
   const int cx = min(max(g0.x, 0), gx - 1), cy = min(max(g0.y, 0), gy - 1), cz = min(max(g0.z, 0), gz - 1);
-  float3 F = make_float3(0.f, 0.f, 0.f);
+  // x and y as FP32 pairs (force_term_xy); xi - xj as fma(xj, -1, xi)
+  const float2 xi_xy = make_float2(xi.x, xi.y), vi_xy = make_float2(vi.x, vi.y);
+  float2 F_xy = make_float2(0.f, 0.f);
+  float F_z = 0.f;
   unsigned long long mnext = masks[i];
 #pragma unroll 1
   for (int r = 0; r < kRows; ++r) {
@@ -624,28 +627,29 @@ k_force_fields(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ po
       // grid's first cell never becomes a 2^32-element pointer offset
       const uint32_t c = d.c_off + (uint32_t)(row + f - 1);
       const uint32_t s0 = __ldg(start + c) + 15u;
-      float3 cell = make_float3(0.f, 0.f, 0.f);
+      float2 cell_xy = make_float2(0.f, 0.f);
+      float cell_z = 0.f;
       do {
         const int b = 31 - __clz(bits);
         bits ^= 1u << b;
         const uint32_t j = s0 - (uint32_t)b;  // candidate 15 - b
         const float4 xj = __ldg(pos + j), vj = __ldg(vel + j);
         const float2 dpj = __ldg(dp + j);
-        const float rx = __fsub_rn(xi.x, xj.x), ry = __fsub_rn(xi.y, xj.y), rz = __fsub_rn(xi.z, xj.z);
-        const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
-        float3 t;
-        if (force_term(k, vi, inv_di, pi, vj, dpj.x, dpj.y, rx, ry, rz, dist2, t)) {
-          cell.x = __fadd_rn(cell.x, t.x);
-          cell.y = __fadd_rn(cell.y, t.y);
-          cell.z = __fadd_rn(cell.z, t.z);
+        const float2 r_xy = __ffma2_rn(make_float2(xj.x, xj.y), make_float2(-1.f, -1.f), xi_xy);
+        const float rz = __fsub_rn(xi.z, xj.z);
+        const float dist2 = __fmaf_rn(rz, rz, __fmaf_rn(r_xy.y, r_xy.y, __fmul_rn(r_xy.x, r_xy.x)));
+        float2 t_xy;
+        float t_z;
+        if (force_term_xy(k, vi_xy, vi.z, inv_di, pi, vj, dpj.x, dpj.y, r_xy, rz, dist2, t_xy, t_z)) {
+          cell_xy = __fadd2_rn(cell_xy, t_xy);
+          cell_z = __fadd_rn(cell_z, t_z);
         }
       } while (bits);
-      F.x = __fadd_rn(F.x, cell.x);
-      F.y = __fadd_rn(F.y, cell.y);
-      F.z = __fadd_rn(F.z, cell.z);
+      F_xy = __fadd2_rn(F_xy, cell_xy);
+      F_z = __fadd_rn(F_z, cell_z);
     }
   }
-  const float3 add = velocity_increment(p, F, xi, vi);
+  const float3 add = velocity_increment(p, make_float3(F_xy.x, F_xy.y, F_z), xi, vi);
   vel_out[i] = make_float4(__fadd_rn(vi.x, add.x), __fadd_rn(vi.y, add.y), __fadd_rn(vi.z, add.z),
                            __fadd_rn(vi.w, 0.f));
 }
