@@ -343,6 +343,76 @@ struct FeatOut {
   const float* stats;       // mean[16], inv_std[16]
 };
 
+// One pair's contribution to the learned step's features (network inputs,
+// BF16: approximate reciprocals suffice).
+__device__ __forceinline__ void feat_add(FeatAcc& fa, const ForceConsts& k, float inv_h, float4 vi, float4 vj,
+                                         float rx, float ry, float rz, float dist2) {
+  const float ir = rsqrtf(fmaxf(dist2, k.minDist * k.minDist));
+  const float r = fmaxf(k.minDist, dist2 * ir);
+  if (r < k.h) {
+    const float q = 1.f - r * inv_h, w = q * q;
+    const float dvx = vj.x - vi.x, dvy = vj.y - vi.y, dvz = vj.z - vi.z;
+    fa.sw += w;
+    fa.n += 1.f;
+    fa.div += w * (dvx * rx + dvy * ry + dvz * rz) * ir;
+    fa.rv[0] += w * dvx;
+    fa.rv[1] += w * dvy;
+    fa.rv[2] += w * dvz;
+    fa.rx[0] -= w * rx;
+    fa.rx[1] -= w * ry;
+    fa.rx[2] -= w * rz;
+  }
+}
+
+// The 16 features of particle i from its accumulated pair sums, its SPH
+// force sum F and its state, raw (FP32) and/or standardised (BF16).
+__device__ __forceinline__ void feature_out(const SimParams& p, const FeatAcc& fa, float3 F, float4 xi, float4 vi,
+                                            float pi, float dens_i, FeatOut fo, uint32_t i) {
+  const float dt = p.timeStep, h = p.h;
+  const float g = sqrtf(p.gravity.x * p.gravity.x + p.gravity.y * p.gravity.y +
+                        p.gravity.z * p.gravity.z) + 1e-6f;
+  const float s = __fmul_rn(p.particleMass, p.timeStep), isw = 1.f / (fa.sw + 1e-6f);
+  float f[16];
+  f[0] = dens_i / p.restDensity - 1.f;
+  f[1] = pi / (p.restDensity * g * h);
+  f[2] = fa.n * (1.f / 64.f);
+  f[3] = fa.div * dt / h;
+  f[4] = fa.rv[0] * isw * dt / h;
+  f[5] = fa.rv[1] * isw * dt / h;
+  f[6] = fa.rv[2] * isw * dt / h;
+  f[7] = fa.rx[0] * isw / h;
+  f[8] = fa.rx[1] * isw / h;
+  f[9] = fa.rx[2] * isw / h;
+  f[10] = F.x * s / (g * dt);
+  f[11] = F.y * s / (g * dt);
+  f[12] = F.z * s / (g * dt);
+  {
+    float3 bx = make_float3(xi.x, xi.y, xi.z), bv = make_float3(vi.x, vi.y, vi.z);
+    boundary(p, bx, bv);
+    f[13] = (bv.x - vi.x) / (g * dt);
+    f[14] = (bv.y - vi.y) / (g * dt);
+    f[15] = (bv.z - vi.z) / (g * dt);
+  }
+  if (fo.raw) {
+    float4* o = reinterpret_cast<float4*>(fo.raw + (size_t)i * 16);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+  }
+  if (fo.norm) {
+    uint32_t u[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float a = (f[2 * q] - fo.stats[2 * q]) * fo.stats[16 + 2 * q];
+      const float b = (f[2 * q + 1] - fo.stats[2 * q + 1]) * fo.stats[16 + 2 * q + 1];
+      __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+      u[q] = *reinterpret_cast<uint32_t*>(&v);
+    }
+    uint4* o = reinterpret_cast<uint4*>(fo.norm + (size_t)i * 16);
+    o[0] = make_uint4(u[0], u[1], u[2], u[3]);
+    o[1] = make_uint4(u[4], u[5], u[6], u[7]);
+  }
+}
+
 template <bool kMask, bool kFeat, bool kNC = true>
 __device__ __forceinline__ void force_item(const SceneDesc* __restrict__ sc,
                                            const uint32_t* __restrict__ poff, int S, uint32_t N,
@@ -369,22 +439,7 @@ __device__ __forceinline__ void force_item(const SceneDesc* __restrict__ sc,
   FeatAcc fa;
   const float inv_h = kFeat ? 1.f / p.h : 0.f;
   auto feat = [&](float4 vj, float rx, float ry, float rz, float dist2) {
-    // network inputs (BF16): approximate reciprocals suffice
-    const float ir = rsqrtf(fmaxf(dist2, k.minDist * k.minDist));
-    const float r = fmaxf(k.minDist, dist2 * ir);
-    if (r < k.h) {
-      const float q = 1.f - r * inv_h, w = q * q;
-      const float dvx = vj.x - vi.x, dvy = vj.y - vi.y, dvz = vj.z - vi.z;
-      fa.sw += w;
-      fa.n += 1.f;
-      fa.div += w * (dvx * rx + dvy * ry + dvz * rz) * ir;
-      fa.rv[0] += w * dvx;
-      fa.rv[1] += w * dvy;
-      fa.rv[2] += w * dvz;
-      fa.rx[0] -= w * rx;
-      fa.rx[1] -= w * ry;
-      fa.rx[2] -= w * rz;
-    }
+    feat_add(fa, k, inv_h, vi, vj, rx, ry, rz, dist2);
   };
   // Pair term of candidate j (the masks already hold dist2 < h2_out):
   // returns whether r < h, with the term in f.
@@ -492,51 +547,7 @@ __device__ __forceinline__ void force_item(const SceneDesc* __restrict__ sc,
   const float3 add = velocity_increment(p, F, xi, vi);
   vel_out[i] = make_float4(__fadd_rn(vi.x, add.x), __fadd_rn(vi.y, add.y), __fadd_rn(vi.z, add.z),
                            __fadd_rn(vi.w, 0.f));
-  if (kFeat) {
-    const float dt = p.timeStep, h = p.h;
-    const float g = sqrtf(p.gravity.x * p.gravity.x + p.gravity.y * p.gravity.y +
-                          p.gravity.z * p.gravity.z) + 1e-6f;
-    const float s = __fmul_rn(p.particleMass, p.timeStep), isw = 1.f / (fa.sw + 1e-6f);
-    float f[16];
-    f[0] = dens[i] / p.restDensity - 1.f;
-    f[1] = pi / (p.restDensity * g * h);
-    f[2] = fa.n * (1.f / 64.f);
-    f[3] = fa.div * dt / h;
-    f[4] = fa.rv[0] * isw * dt / h;
-    f[5] = fa.rv[1] * isw * dt / h;
-    f[6] = fa.rv[2] * isw * dt / h;
-    f[7] = fa.rx[0] * isw / h;
-    f[8] = fa.rx[1] * isw / h;
-    f[9] = fa.rx[2] * isw / h;
-    f[10] = F.x * s / (g * dt);
-    f[11] = F.y * s / (g * dt);
-    f[12] = F.z * s / (g * dt);
-    {
-      float3 bx = make_float3(xi.x, xi.y, xi.z), bv = make_float3(vi.x, vi.y, vi.z);
-      boundary(p, bx, bv);
-      f[13] = (bv.x - vi.x) / (g * dt);
-      f[14] = (bv.y - vi.y) / (g * dt);
-      f[15] = (bv.z - vi.z) / (g * dt);
-    }
-    if (fo.raw) {
-      float4* o = reinterpret_cast<float4*>(fo.raw + (size_t)i * 16);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) o[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
-    }
-    if (fo.norm) {
-      uint32_t u[8];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const float a = (f[2 * q] - fo.stats[2 * q]) * fo.stats[16 + 2 * q];
-        const float b = (f[2 * q + 1] - fo.stats[2 * q + 1]) * fo.stats[16 + 2 * q + 1];
-        __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
-        u[q] = *reinterpret_cast<uint32_t*>(&v);
-      }
-      uint4* o = reinterpret_cast<uint4*>(fo.norm + (size_t)i * 16);
-      o[0] = make_uint4(u[0], u[1], u[2], u[3]);
-      o[1] = make_uint4(u[4], u[5], u[6], u[7]);
-    }
-  }
+  if (kFeat) feature_out(p, fa, F, xi, vi, pi, dens[i], fo, i);
 }
 
 // Which thread of the block runs which of its particles does not change a
@@ -1265,7 +1276,11 @@ template <int kThreads>
 void launch_force(SphSystem* s, cudaStream_t st, int b, int v, const StepOpts& o, int kind) {
   const unsigned g = grid_for(s->N, kThreads);
   constexpr int kMin = 1024 / kThreads;
-  if (o.feat)  // the featured pass of the learned step: the global row walk
+  if (o.feat && kind == 2)  // the featured pass of the learned step: by cell fields
+    k_force_fields<kThreads, kMin * 7 / 8, true><<<g, kThreads, 0, st>>>(
+        o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dp, s->start, s->masks, s->vel[v],
+        s->dens, o.fo);
+  else if (o.feat)  // the featured pass of the learned step: the global row walk
     k_force<true, 128, 8, true><<<grid_for(s->N, 128), 128, 0, st>>>(
         o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->dp, s->start, s->count,
         s->masks, s->vel[v], o.fo);
@@ -1274,8 +1289,9 @@ void launch_force(SphSystem* s, cudaStream_t st, int b, int v, const StepOpts& o
         o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dens, s->dp, s->start, s->count,
         s->masks, s->vel[v], kTileForceSlots);
   else if (kind == 2)
-    k_force_fields<kThreads, kMin><<<g, kThreads, 0, st>>>(o.scenes, s->d_poff, s->S, s->N, s->pos[b],
-                                                           s->vel[1 - v], s->dp, s->start, s->masks, s->vel[v]);
+    k_force_fields<kThreads, kMin, false><<<g, kThreads, 0, st>>>(o.scenes, s->d_poff, s->S, s->N, s->pos[b],
+                                                                  s->vel[1 - v], s->dp, s->start, s->masks,
+                                                                  s->vel[v], nullptr, FeatOut{});
   else if (kind == 3 && kThreads <= 128)
     k_force_coop<kThreads <= 128 ? kThreads : 128><<<g, kThreads, 0, st>>>(
         o.scenes, s->d_poff, s->S, s->N, s->pos[b], s->vel[1 - v], s->dp, s->start, s->masks, s->vel[v]);

@@ -589,12 +589,16 @@ k_density_pairs(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ p
 // highest first with 32-bit operations, and its partial sum is added to the
 // total when its bits are done (a cell without a set bit would add +0, which
 // changes nothing, so it is skipped).
-template <int kThreads, int kMinBlocks>
+// With kFeat (the learned step's coarse step) it also accumulates the pair
+// sums of the 16 features in the same walk order as force_item and writes
+// them (feature_out), so the features equal the row walk's.
+template <int kThreads, int kMinBlocks, bool kFeat>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
 k_force_fields(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ poff, int S, uint32_t N,
                const float4* __restrict__ pos, const float4* __restrict__ vel,
                const float2* __restrict__ dp, const uint32_t* __restrict__ start,
-               const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out) {
+               const unsigned long long* __restrict__ masks, float4* __restrict__ vel_out,
+               const float* __restrict__ dens, FeatOut fo) {
   const uint32_t i = regrouped_particle<kThreads>(sc, poff, S, N, pos);
   if (i >= N) return;
   const SceneDesc& d = sc[S == 1 ? 0 : scene_of(poff, S, i)];
@@ -610,6 +614,8 @@ k_force_fields(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ po
   const float2 xi_xy = make_float2(xi.x, xi.y), vi_xy = make_float2(vi.x, vi.y);
   float2 F_xy = make_float2(0.f, 0.f);
   float F_z = 0.f;
+  FeatAcc fa;
+  const float inv_h = kFeat ? 1.f / p.h : 0.f;
   unsigned long long mnext = masks[i];
 #pragma unroll 1
   for (int r = 0; r < kRows; ++r) {
@@ -644,6 +650,7 @@ k_force_fields(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ po
           cell_xy = __fadd2_rn(cell_xy, t_xy);
           cell_z = __fadd_rn(cell_z, t_z);
         }
+        if (kFeat) feat_add(fa, k, inv_h, vi, vj, r_xy.x, r_xy.y, rz, dist2);
       } while (bits);
       F_xy = __fadd2_rn(F_xy, cell_xy);
       F_z = __fadd_rn(F_z, cell_z);
@@ -652,6 +659,7 @@ k_force_fields(const SceneDesc* __restrict__ sc, const uint32_t* __restrict__ po
   const float3 add = velocity_increment(p, make_float3(F_xy.x, F_xy.y, F_z), xi, vi);
   vel_out[i] = make_float4(__fadd_rn(vi.x, add.x), __fadd_rn(vi.y, add.y), __fadd_rn(vi.z, add.z),
                            __fadd_rn(vi.w, 0.f));
+  if (kFeat) feature_out(p, fa, make_float3(F_xy.x, F_xy.y, F_z), xi, vi, pi, dens[i], fo, i);
 }
 
 // ---- force, warp-cooperative by rows --------------------------------------------

@@ -34,6 +34,29 @@ def test_features(cuda):
     assert f[:, 2].max() > 0.2  # neighbour counts / 64
 
 
+def test_featured_walks_agree(cuda):
+    """The featured force pass of the field walk (walk shape 4) and of the
+    row walk (shape 1) accumulate the same sums in the same order: features,
+    ids and the learned steps that follow are the same bits."""
+    torch = cuda
+    w = configs.dambreak_small(side=32)
+    model = learned.Model.load()
+    out = {}
+    for shape in (1, 4):
+        with _sys(w.xml, w.pos, w.vel) as s:
+            s.set_walk_shape(shape)
+            s.update(30)
+            f = torch.empty((s.n, 16), dtype=torch.float32, device="cuda")
+            ids = torch.empty(s.n, dtype=torch.int32, device="cuda")
+            learned.features_step(s, f, ids)
+            model.install(s)
+            fb = learned.learned_step(s, 10, 4, 0.02)
+            out[shape] = (f.cpu().numpy(), ids.cpu().numpy(), s.get_array(ARRAY_POS),
+                          s.get_array(ARRAY_VEL), fb)
+    for a, b in zip(out[1], out[4]):
+        assert np.array_equal(a, b)
+
+
 def test_fallback_reproduces_fine_steps(cuda):
     """With tol = 0 every coarse step fails the density check, is undone and
     replaced by 4 plain steps: the result equals 12 plain steps bit for bit."""
