@@ -38,6 +38,19 @@ size_t scan_scratch_words(size_t n);
 // `scratch` holds scan_scratch_words(n) uint32 words.
 int exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* scratch,
                    cudaStream_t stream);
+// Lists of the elements (cells) whose value (particle count) exceeds
+// min_list: those up to mid_max into `mid`, the larger into `big`, the list
+// lengths in counters[0] and counters[1] (order within a list unspecified).
+struct ScanLists {
+  uint32_t min_list, mid_max;
+  uint32_t *mid, *big, *counters;
+};
+// exclusive_scan that also builds `lists` while it scans, in the same two
+// launches.  The scan's ticket counter (scratch[0]) must be zero on entry,
+// as it is after every scan (the last block clears it): the caller zeroes
+// it once when it allocates the scratch.
+int exclusive_scan_lists(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* scratch,
+                         const ScanLists& lists, cudaStream_t stream);
 
 // ---- stable LSD radix sort of (key, value) pairs (sph_scan.cu) ----------
 size_t radix_scratch_words(size_t n);

@@ -76,7 +76,7 @@ __device__ __forceinline__ void load16(const uint32_t* in, uint32_t n, size_t fi
 
 __global__ void __launch_bounds__(kThreads)
 scan_tile_sums(const uint32_t* __restrict__ in, uint32_t n, uint32_t* __restrict__ counter,
-               uint32_t* __restrict__ tile_sum, uint32_t tiles) {
+               uint32_t* __restrict__ tile_sum, uint32_t tiles, uint32_t* __restrict__ list_counters) {
   __shared__ uint32_t warp_tot[32];
   __shared__ uint32_t ticket;
   const size_t first = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kPerThread;
@@ -105,12 +105,15 @@ scan_tile_sums(const uint32_t* __restrict__ in, uint32_t n, uint32_t* __restrict
     if (i < tiles) tile_sum[i] = carry + e;
     carry += t;
   }
-  if (threadIdx.x == 0) *counter = 0;  // ready for the next scan
+  if (threadIdx.x == 0) {
+    *counter = 0;  // ready for the next scan
+    if (list_counters) list_counters[0] = list_counters[1] = 0;  // filled by scan_tiles
+  }
 }
 
 __global__ void __launch_bounds__(kThreads)
 scan_tiles(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint32_t n,
-           const uint32_t* __restrict__ tile_sum) {
+           const uint32_t* __restrict__ tile_sum, ScanLists lists) {
   __shared__ uint32_t warp_tot[32];
   const size_t first = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kPerThread;
   uint32_t v[16];
@@ -134,6 +137,34 @@ scan_tiles(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint32_t
 #pragma unroll
     for (int k = 0; k < 16; ++k)
       if (first + k < n) out[first + k] = o[k];
+  }
+  if (lists.counters) {
+    // the elements above min_list: the block's counts of each kind scanned
+    // together (mid in the low 16 bits, big in the high: at most 4096 each),
+    // one atomic per list and block, then each thread writes its own
+    uint32_t nm = 0, nb = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      nm += v[k] > lists.min_list && v[k] <= lists.mid_max;
+      nb += v[k] > lists.mid_max;
+    }
+    uint32_t tot;
+    const uint32_t pre = block_exclusive_scan(nm | (nb << 16), warp_tot, &tot);
+    __shared__ uint32_t base_m, base_b;
+    if (threadIdx.x == 0) {
+      base_m = (tot & 0xFFFFu) ? atomicAdd(lists.counters + 0, tot & 0xFFFFu) : 0u;
+      base_b = (tot >> 16) ? atomicAdd(lists.counters + 1, tot >> 16) : 0u;
+    }
+    __syncthreads();
+    uint32_t om = base_m + (pre & 0xFFFFu), ob = base_b + (pre >> 16);
+    if (nm | nb) {
+#pragma unroll 1
+      for (int k = 0; k < 16; ++k) {
+        const uint32_t e = (uint32_t)(first + k);
+        if (v[k] > lists.mid_max) lists.big[ob++] = e;
+        else if (v[k] > lists.min_list) lists.mid[om++] = e;
+      }
+    }
   }
 }
 
@@ -210,8 +241,17 @@ int exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* scra
   uint32_t* counter = scratch;
   uint32_t* tile_sum = scratch + 1;
   SPH_CUDA(cudaMemsetAsync(counter, 0, sizeof(uint32_t), stream), "scan counter reset");
-  scan_tile_sums<<<tiles, kThreads, 0, stream>>>(in, n, counter, tile_sum, tiles);
-  scan_tiles<<<tiles, kThreads, 0, stream>>>(in, out, n, tile_sum);
+  scan_tile_sums<<<tiles, kThreads, 0, stream>>>(in, n, counter, tile_sum, tiles, nullptr);
+  scan_tiles<<<tiles, kThreads, 0, stream>>>(in, out, n, tile_sum, ScanLists{0, 0, nullptr, nullptr, nullptr});
+  return cuda_check(cudaGetLastError(), "scan kernels");
+}
+
+int exclusive_scan_lists(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* scratch,
+                         const ScanLists& lists, cudaStream_t stream) {
+  if (n == 0) return SPH_OK;
+  const uint32_t tiles = tiles_for(n);
+  scan_tile_sums<<<tiles, kThreads, 0, stream>>>(in, n, scratch, scratch + 1, tiles, lists.counters);
+  scan_tiles<<<tiles, kThreads, 0, stream>>>(in, out, n, scratch + 1, lists);
   return cuda_check(cudaGetLastError(), "scan kernels");
 }
 

@@ -16,11 +16,11 @@
 // One step (cSPH::Update, SPH_Update.cpp:12-81):
 //   k_integrate_count  integrate each particle (in registers), find its cell,
 //                      take a rank in the cell with one atomic per warp group
-//   exclusive scan     count -> start
+//   exclusive scan     count -> start, and the lists of the cells with
+//                      more than 32 particles
 //   k_scatter_ids      slot[start + rank] = original index
-//   k_find_cells,      the id segments of cells with more than 32 particles
-//   k_sort_cells,      sorted (a warp, a block, or a block over global
-//   k_sort_big_cells   scratch, by size)
+//   k_sort_cells,      the id segments of the listed cells sorted (a warp,
+//   k_sort_big_cells   a block, or a block over global scratch, by size)
 //   k_place            stable position inside the cell = number of smaller
 //                      original indices there (the reference's sort is
 //                      stable on original order); integrate again and write
@@ -1363,12 +1363,14 @@ int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr,
   k_integrate_count<<<gN, kBlock, 0, st>>>(sc, s->d_poff, s->S, s->N, s->pos[a], s->vel[v],
                                            s->key, s->rank, s->count, s->flags);
   mark();
-  SPH_TRY(exclusive_scan(s->count, s->start, s->C, s->scan_tmp, st));
+  // the scan also lists the cells whose id segments need sorting (more than
+  // kLinearRank particles: up to kWarpSortMax into sort_list, the rest into
+  // big_list)
+  SPH_TRY(exclusive_scan_lists(s->count, s->start, s->C, s->scan_tmp,
+                               ScanLists{kLinearRank, kWarpSortMax, s->sort_list, s->big_list, s->sort_counters},
+                               st));
   mark();
   k_scatter_ids<<<gN, kBlock, 0, st>>>(s->N, s->key, s->rank, s->id[a], s->start, s->slot);
-  SPH_CUDA(cudaMemsetAsync(s->sort_counters, 0, 2 * sizeof(uint32_t), st), "step: clear sort lists");
-  k_find_cells<<<grid_for(s->C, kBlock), kBlock, 0, st>>>(s->C, s->count, kLinearRank,
-                                                          s->sort_list, s->sort_counters, s->big_list);
   k_sort_cells<<<s->sort_blocks, kSortWarps * 32, 0, st>>>(s->start, s->count, s->slot,
                                                            s->sort_list, s->sort_counters, s->dest);
   k_sort_big_cells<<<s->big_blocks, kBigThreads, kBlockSortMax * sizeof(uint32_t), st>>>(
@@ -1510,6 +1512,7 @@ int create(const SimParams* scenes, uint32_t count, SphSystem** out) {
     cudaMemsetAsync(s->flags, 0, sizeof(uint32_t), s->stream);
     cudaMemsetAsync(s->dens, 0, sizeof(float) * n, s->stream);
     cudaMemsetAsync(s->pres, 0, sizeof(float) * n, s->stream);
+    cudaMemsetAsync(s->scan_tmp, 0, sizeof(uint32_t), s->stream);  // the scan's ticket counter
     k_iota<<<grid_for(n, kBlock), kBlock, 0, s->stream>>>(s->id[0], (uint32_t)n);
     rc = cuda_check(cudaGetLastError(), "init");
   }
