@@ -55,8 +55,8 @@ STAGE_BYTES = {  # stage: (bytes per particle, bytes per cell)
     "density": (24, 8),
     "force": (56, 8),
 }
-KERNELS_PER_STEP = 10  # integrate_count, 2 scan kernels, scatter_ids, find_cells, sort_cells,
-#                       sort_big_cells, place, density, force
+KERNELS_PER_STEP = 9  # integrate_count, 2 scan kernels (which also list the crowded cells),
+#                      scatter_ids, sort_cells, sort_big_cells, place, density, force
 
 
 def log(*a):
