@@ -1142,6 +1142,10 @@ struct SphSystem {
   cudaStream_t stream = nullptr;
   bool own_stream = false;  // created here (destroyed here) or borrowed
   cudaStream_t cap_stream = nullptr;
+  // the sort of the largest cells runs beside the warp sorts: a side stream
+  // forked from and joined back into the step's stream by two events
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // graph_steps steps, keyed by cp at launch
   uint32_t graph_steps = 2;                         // steps per captured graph (even)
   int walk_shape = kDefaultShape;                   // index into kShapes
@@ -1371,10 +1375,16 @@ int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr,
                                st));
   mark();
   k_scatter_ids<<<gN, kBlock, 0, st>>>(s->N, s->key, s->rank, s->id[a], s->start, s->slot);
+  // the few cells above kWarpSortMax (a block each) beside the warp sorts:
+  // the two kernels sort disjoint cells
+  SPH_CUDA(cudaEventRecord(s->fork_ev, st), "step: fork");
+  SPH_CUDA(cudaStreamWaitEvent(s->side, s->fork_ev, 0), "step: fork");
+  k_sort_big_cells<<<s->big_blocks, kBigThreads, kBlockSortMax * sizeof(uint32_t), s->side>>>(
+      s->start, s->count, s->slot, s->big_list, s->sort_counters + 1, s->sort_scratch, s->dest);
+  SPH_CUDA(cudaEventRecord(s->join_ev, s->side), "step: join");
   k_sort_cells<<<s->sort_blocks, kSortWarps * 32, 0, st>>>(s->start, s->count, s->slot,
                                                            s->sort_list, s->sort_counters, s->dest);
-  k_sort_big_cells<<<s->big_blocks, kBigThreads, kBlockSortMax * sizeof(uint32_t), st>>>(
-      s->start, s->count, s->slot, s->big_list, s->sort_counters + 1, s->sort_scratch, s->dest);
+  SPH_CUDA(cudaStreamWaitEvent(st, s->join_ev, 0), "step: join");
   mark();
   k_place<<<gN, kBlock, 0, st>>>(sc, s->d_poff, s->S, s->N, s->pos[a], s->vel[v], s->id[a],
                                  s->key, s->start, s->count, s->slot, s->dest, s->pos[b], s->vel[1 - v],
@@ -1425,6 +1435,9 @@ void free_all(SphSystem* s) {
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+  if (s->side) cudaStreamDestroy(s->side);
+  if (s->fork_ev) cudaEventDestroy(s->fork_ev);
+  if (s->join_ev) cudaEventDestroy(s->join_ev);
   if (s->stats_host) cudaFreeHost(s->stats_host);
 }
 
@@ -1491,6 +1504,9 @@ int create(const SimParams* scenes, uint32_t count, SphSystem** out) {
 #undef ALLOC
   if (rc == SPH_OK) rc = cuda_check(cudaStreamCreate(&s->stream), "stream");
   s->own_stream = rc == SPH_OK;
+  if (rc == SPH_OK) rc = cuda_check(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking), "side stream");
+  if (rc == SPH_OK) rc = cuda_check(cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming), "fork event");
+  if (rc == SPH_OK) rc = cuda_check(cudaEventCreateWithFlags(&s->join_ev, cudaEventDisableTiming), "join event");
   if (rc == SPH_OK)
     rc = cuda_check(cudaFuncSetAttribute(k_sort_big_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(kBlockSortMax * sizeof(uint32_t))),
