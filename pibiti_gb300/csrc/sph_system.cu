@@ -220,7 +220,6 @@ static_assert(kWalkShapes == SPH_WALK_SHAPES, "walk shapes in pibiti_sph.h");
 // somewhere else reads the same masks.
 constexpr int kRows = 9;
 constexpr uint32_t kMaskMaxPerCell = 16;
-constexpr int kMaskField = 16;
 #ifndef SPH_WALK_MASKS
 #define SPH_WALK_MASKS 1  // 0: no mask buffer (saves 72 B per particle)
 #endif
