@@ -390,6 +390,25 @@ def test_walk_shapes_and_graph_lengths_agree(cuda):
                 np.testing.assert_array_equal(out[1], ref[1])
 
 
+@pytest.mark.parametrize("case", ["features", "truncate", "rotor", "propeller", "hmapxz", "hmapyz", "bigrid"])
+def test_walk_shapes_agree_on_golden_scenes(cuda, golden, case):
+    """The golden scenes (colliders, accelerators, rotors, height maps,
+    truncated cells, a 32-bit hash grid) step to the same bits with every
+    walk shape as with the default one, which test_step_vs_reference checks
+    against the reference."""
+    g = golden(f"step_{case}.npz")
+    p = params_from(g["params"])
+    outs = []
+    for shape in range(len(SPH.WALK_THREADS)):
+        with system_from(p, g["pos_in"], g["vel_in"]) as s:
+            s.set_walk_shape(shape)
+            s.update(2)
+            outs.append((s.get_array(ARRAY_POS), s.get_array(ARRAY_VEL), s.fields()[0]))
+    for o in outs[1:]:
+        for a, b in zip(o, outs[0]):
+            np.testing.assert_array_equal(a, b)
+
+
 def test_staged_walks_match_global_walks_on_sparse_particles(cuda):
     """Particles strewn over many cells: blocks of the staged walks whose
     cells span too large a box walk global memory instead; every shape gives
