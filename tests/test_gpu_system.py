@@ -164,9 +164,12 @@ def test_stats_reductions_at_1m(cuda):
     assert st[3] == 0
 
 
-def test_ensemble_equals_separate_runs(cuda):
+@pytest.mark.parametrize("shape", [1, 4, 9])
+def test_ensemble_equals_separate_runs(cuda, shape):
     """Three scenes of different size and parameters in one handle give the
-    same bits as three separate handles."""
+    same bits as three separate handles (with a global, the default staged
+    and the warp-cooperative walk: staged blocks over two scenes walk global
+    memory)."""
     ws = [configs.dambreak_small(side=s, seed=i) for i, s in enumerate((8, 12, 16))]
     ps = []
     for i, w in enumerate(ws):
@@ -175,6 +178,7 @@ def test_ensemble_equals_separate_runs(cuda):
         p.viscosity = 2.0 + i
         ps.append(p)
     with SPH(ps) as e:
+        e.set_walk_shape(shape)
         e.set_array(ARRAY_POS, np.concatenate([w.pos for w in ws]))
         e.set_array(ARRAY_VEL, np.concatenate([w.vel for w in ws]))
         e.update(20)
