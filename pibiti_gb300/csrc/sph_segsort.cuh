@@ -189,6 +189,109 @@ k_sort_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict__ co
   }
 }
 
+// Ranks of distinct ids (particle ids of one cell) without sorting them:
+// rank(id) = the number of the cell's ids below it, and dest_of[id] =
+// s0 + rank.  One warp per listed segment of up to kWarpSortMax ids:
+//   1. bucket(id) = floor((id - lo) * B / (hi - lo + 1)), B = kRankBuckets,
+//      lo and hi the segment's smallest and largest id; in floating point,
+//      which keeps the function non-decreasing in id (every step rounds
+//      monotonically), so all ids of a lower bucket are smaller;
+//   2. counts per bucket (shared-memory atomics), exclusive scan of them;
+//   3. each id placed into its bucket's range of a shared array;
+//   4. rank = the start of its bucket + the ids of its own bucket below it.
+// The work is linear in the segment as long as the buckets stay small; a
+// segment whose fullest bucket holds more than kRankBucketMax ids (ids
+// bunched against an outlier) is sorted instead, by the shared-memory
+// bitonic network in the same warp (warp_sort_segment_smem).
+// Bucket b's counter sits at b + b / 32 so that a lane reading its own 32
+// consecutive counters meets no bank conflict.
+constexpr uint32_t kRankBuckets = 1024, kRankBucketMax = 32, kRankWarps = 4;
+constexpr uint32_t kRankPadded = kRankBuckets + kRankBuckets / 32;
+__device__ __forceinline__ uint32_t rank_slot(uint32_t b) { return b + (b >> 5); }
+
+__global__ void __launch_bounds__(kRankWarps * 32)
+k_rank_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
+             const uint32_t* __restrict__ slot, const uint32_t* __restrict__ list,
+             const uint32_t* __restrict__ counters, uint32_t* __restrict__ dest_of) {
+  __shared__ uint32_t sm[kRankWarps][kRankPadded + kWarpSortMax];
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t* hist = sm[w];
+  uint32_t* tmp = sm[w] + kRankPadded;
+  const uint32_t nl = counters[0];
+  for (uint32_t q = blockIdx.x * kRankWarps + w; q < nl; q += gridDim.x * kRankWarps) {
+    const uint32_t c = list[q], s0 = start[c], n = count[c];
+    uint32_t v[32];
+    uint32_t lo = 0xffffffffu, hi = 0u;
+#pragma unroll
+    for (int e = 0; e < 32; ++e) {  // coalesced loads
+      const uint32_t k = 32u * e + lane;
+      v[e] = k < n ? slot[s0 + k] : 0u;
+      if (k < n) {
+        lo = min(lo, v[e]);
+        hi = max(hi, v[e]);
+      }
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    const float scale = (float)kRankBuckets / ((float)(hi - lo) + 1.f);
+    auto bucket = [&](uint32_t id) {
+      return min((uint32_t)((float)(id - lo) * scale), kRankBuckets - 1u);
+    };
+#pragma unroll
+    for (uint32_t t = 0; t < kRankPadded; t += 32)
+      if (t + lane < kRankPadded) hist[t + lane] = 0u;
+    __syncwarp();
+#pragma unroll
+    for (int e = 0; e < 32; ++e)
+      if (32u * e + lane < n) atomicAdd(&hist[rank_slot(bucket(v[e]))], 1u);
+    __syncwarp();
+    // this lane's buckets 32 * lane .. 32 * lane + 31: largest and total
+    uint32_t sum = 0u, most = 0u;
+#pragma unroll
+    for (int t = 0; t < 32; ++t) {
+      const uint32_t k = hist[rank_slot(32u * lane + t)];
+      sum += k;
+      most = max(most, k);
+    }
+    if (__reduce_max_sync(0xffffffffu, most) > kRankBucketMax) {
+      // reads slot only, since dest_of is given
+      warp_sort_segment_smem(const_cast<uint32_t*>(slot), s0, n, lane, dest_of, tmp);
+      continue;
+    }
+    // exclusive scan over all buckets: the lanes' totals, then within a lane
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if ((int)lane >= o) x += y;
+    }
+    uint32_t run = x - sum;
+#pragma unroll
+    for (int t = 0; t < 32; ++t) {
+      const uint32_t k = hist[rank_slot(32u * lane + t)];
+      hist[rank_slot(32u * lane + t)] = run;
+      run += k;
+    }
+    __syncwarp();
+    // into the buckets' ranges; afterwards hist[bucket b] = the end of b
+#pragma unroll
+    for (int e = 0; e < 32; ++e)
+      if (32u * e + lane < n) tmp[atomicAdd(&hist[rank_slot(bucket(v[e]))], 1u)] = v[e];
+    __syncwarp();
+#pragma unroll
+    for (int e = 0; e < 32; ++e) {
+      if (32u * e + lane < n) {
+        const uint32_t b = bucket(v[e]);
+        const uint32_t b0 = b ? hist[rank_slot(b - 1u)] : 0u, b1 = hist[rank_slot(b)];
+        uint32_t r = b0;
+        for (uint32_t t = b0; t < b1; ++t) r += tmp[t] < v[e];
+        dest_of[v[e]] = s0 + r;
+      }
+    }
+    __syncwarp();  // the next segment reuses hist and tmp
+  }
+}
+
 __global__ void __launch_bounds__(kBigThreads)
 k_sort_big_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
                  uint32_t* __restrict__ slot, const uint32_t* __restrict__ big_list,

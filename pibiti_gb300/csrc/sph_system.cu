@@ -1381,8 +1381,10 @@ int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr,
   k_sort_big_cells<<<s->big_blocks, kBigThreads, kBlockSortMax * sizeof(uint32_t), s->side>>>(
       s->start, s->count, s->slot, s->big_list, s->sort_counters + 1, s->sort_scratch, s->dest);
   SPH_CUDA(cudaEventRecord(s->join_ev, s->side), "step: join");
-  k_sort_cells<<<s->sort_blocks, kSortWarps * 32, 0, st>>>(s->start, s->count, s->slot,
-                                                           s->sort_list, s->sort_counters, s->dest);
+  // cells of up to kWarpSortMax ids: ranked by buckets (k_rank_cells; the
+  // few whose ids bunch into one bucket are sorted by the same warp)
+  k_rank_cells<<<s->sort_blocks, kRankWarps * 32, 0, st>>>(s->start, s->count, s->slot, s->sort_list,
+                                                          s->sort_counters, s->dest);
   SPH_CUDA(cudaStreamWaitEvent(st, s->join_ev, 0), "step: join");
   mark();
   k_place<<<gN, kBlock, 0, st>>>(sc, s->d_poff, s->S, s->N, s->pos[a], s->vel[v], s->id[a],
