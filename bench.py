@@ -56,7 +56,7 @@ STAGE_BYTES = {  # stage: (bytes per particle, bytes per cell)
     "force": (56, 8),
 }
 KERNELS_PER_STEP = 9  # integrate_count, 2 scan kernels (which also list the crowded cells),
-#                      scatter_ids, rank_cells, sort_big_cells, place, density, force
+#                      scatter_ids, rank_cells, rank_big_cells, place, density, force
 
 
 def log(*a):

@@ -191,106 +191,175 @@ k_sort_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict__ co
 
 // Ranks of distinct ids (particle ids of one cell) without sorting them:
 // rank(id) = the number of the cell's ids below it, and dest_of[id] =
-// s0 + rank.  One warp per listed segment of up to kWarpSortMax ids:
-//   1. bucket(id) = floor((id - lo) * B / (hi - lo + 1)), B = kRankBuckets,
-//      lo and hi the segment's smallest and largest id; in floating point,
-//      which keeps the function non-decreasing in id (every step rounds
+// s0 + rank.  One thread block per segment:
+//   1. bucket(id) = floor((id - lo) * B / (hi - lo + 1)), B buckets, lo and
+//      hi the segment's smallest and largest id; in floating point, which
+//      keeps the function non-decreasing in id (every step rounds
 //      monotonically), so all ids of a lower bucket are smaller;
 //   2. counts per bucket (shared-memory atomics), exclusive scan of them;
 //   3. each id placed into its bucket's range of a shared array;
 //   4. rank = the start of its bucket + the ids of its own bucket below it.
-// The work is linear in the segment as long as the buckets stay small; a
-// segment whose fullest bucket holds more than kRankBucketMax ids (ids
-// bunched against an outlier) is sorted instead, by the shared-memory
-// bitonic network in the same warp (warp_sort_segment_smem).
-// Bucket b's counter sits at b + b / 32 so that a lane reading its own 32
-// consecutive counters meets no bank conflict.
-constexpr uint32_t kRankBuckets = 1024, kRankBucketMax = 32, kRankWarps = 4;
-constexpr uint32_t kRankPadded = kRankBuckets + kRankBuckets / 32;
+// The work is linear in the segment as long as the buckets stay small; when
+// the fullest bucket holds more than kRankBucketMax ids (ids bunched against
+// an outlier) block_rank_segment returns false and the caller sorts the
+// segment instead.  Bucket b's counter sits at b + b / 32, so that threads
+// reading runs of consecutive counters meet few bank conflicts.
+constexpr uint32_t kRankBucketMax = 32;
+constexpr uint32_t kRankThreads = 256, kRankBuckets = 1024;  // cells of up to kWarpSortMax ids
+constexpr uint32_t kBigRankBuckets = 4096;                   // cells of up to kBlockSortMax ids
+__host__ __device__ constexpr uint32_t rank_padded(uint32_t buckets) { return buckets + buckets / 32; }
 __device__ __forceinline__ uint32_t rank_slot(uint32_t b) { return b + (b >> 5); }
 
-__global__ void __launch_bounds__(kRankWarps * 32)
-k_rank_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
-             const uint32_t* __restrict__ slot, const uint32_t* __restrict__ list,
-             const uint32_t* __restrict__ counters, uint32_t* __restrict__ dest_of) {
-  __shared__ uint32_t sm[kRankWarps][kRankPadded + kWarpSortMax];
-  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint32_t* hist = sm[w];
-  uint32_t* tmp = sm[w] + kRankPadded;
-  const uint32_t nl = counters[0];
-  for (uint32_t q = blockIdx.x * kRankWarps + w; q < nl; q += gridDim.x * kRankWarps) {
-    const uint32_t c = list[q], s0 = start[c], n = count[c];
-    uint32_t v[32];
-    uint32_t lo = 0xffffffffu, hi = 0u;
+// Block-wide reductions and exclusive scan (blockDim.x a multiple of 32, at
+// most 1024); `red` holds 32 words, and each call ends with a barrier.
+__device__ __forceinline__ uint32_t block_min_max(uint32_t v, bool is_max, uint32_t* red) {
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = is_max ? __reduce_max_sync(0xffffffffu, v) : __reduce_min_sync(0xffffffffu, v);
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  uint32_t x = lane < nw ? red[lane] : (is_max ? 0u : 0xffffffffu);
+  x = is_max ? __reduce_max_sync(0xffffffffu, x) : __reduce_min_sync(0xffffffffu, x);
+  __syncthreads();
+  return x;
+}
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* red) {
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t x = v;
 #pragma unroll
-    for (int e = 0; e < 32; ++e) {  // coalesced loads
-      const uint32_t k = 32u * e + lane;
-      v[e] = k < n ? slot[s0 + k] : 0u;
-      if (k < n) {
-        lo = min(lo, v[e]);
-        hi = max(hi, v[e]);
-      }
-    }
-    lo = __reduce_min_sync(0xffffffffu, lo);
-    hi = __reduce_max_sync(0xffffffffu, hi);
-    const float scale = (float)kRankBuckets / ((float)(hi - lo) + 1.f);
-    auto bucket = [&](uint32_t id) {
-      return min((uint32_t)((float)(id - lo) * scale), kRankBuckets - 1u);
-    };
-#pragma unroll
-    for (uint32_t t = 0; t < kRankPadded; t += 32)
-      if (t + lane < kRankPadded) hist[t + lane] = 0u;
-    __syncwarp();
-#pragma unroll
-    for (int e = 0; e < 32; ++e)
-      if (32u * e + lane < n) atomicAdd(&hist[rank_slot(bucket(v[e]))], 1u);
-    __syncwarp();
-    // this lane's buckets 32 * lane .. 32 * lane + 31: largest and total
-    uint32_t sum = 0u, most = 0u;
-#pragma unroll
-    for (int t = 0; t < 32; ++t) {
-      const uint32_t k = hist[rank_slot(32u * lane + t)];
-      sum += k;
-      most = max(most, k);
-    }
-    if (__reduce_max_sync(0xffffffffu, most) > kRankBucketMax) {
-      // reads slot only, since dest_of is given
-      warp_sort_segment_smem(const_cast<uint32_t*>(slot), s0, n, lane, dest_of, tmp);
-      continue;
-    }
-    // exclusive scan over all buckets: the lanes' totals, then within a lane
-    uint32_t x = sum;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if ((int)lane >= o) x += y;
+  }
+  if (lane == 31) red[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t t = lane < nw ? red[lane] : 0u;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if ((int)lane >= o) x += y;
+      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if ((int)lane >= o) t += y;
     }
-    uint32_t run = x - sum;
-#pragma unroll
-    for (int t = 0; t < 32; ++t) {
-      const uint32_t k = hist[rank_slot(32u * lane + t)];
-      hist[rank_slot(32u * lane + t)] = run;
-      run += k;
-    }
-    __syncwarp();
-    // into the buckets' ranges; afterwards hist[bucket b] = the end of b
-#pragma unroll
-    for (int e = 0; e < 32; ++e)
-      if (32u * e + lane < n) tmp[atomicAdd(&hist[rank_slot(bucket(v[e]))], 1u)] = v[e];
-    __syncwarp();
-#pragma unroll
-    for (int e = 0; e < 32; ++e) {
-      if (32u * e + lane < n) {
-        const uint32_t b = bucket(v[e]);
-        const uint32_t b0 = b ? hist[rank_slot(b - 1u)] : 0u, b1 = hist[rank_slot(b)];
-        uint32_t r = b0;
-        for (uint32_t t = b0; t < b1; ++t) r += tmp[t] < v[e];
-        dest_of[v[e]] = s0 + r;
-      }
-    }
-    __syncwarp();  // the next segment reuses hist and tmp
+    if (lane < nw) red[lane] = t;  // inclusive prefixes of the warps' totals
+  }
+  __syncthreads();
+  const uint32_t before = w ? red[w - 1] : 0u;
+  __syncthreads();
+  return before + x - v;
+}
+
+// hist: rank_padded(kB) words, tmp: >= n words, red: 32 words.  Uniform
+// over the block; false when a bucket is too full (nothing written then).
+template <uint32_t kB>
+__device__ bool block_rank_segment(const uint32_t* __restrict__ slot, uint32_t s0, uint32_t n,
+                                   uint32_t* __restrict__ dest_of, uint32_t* hist, uint32_t* tmp,
+                                   uint32_t* red) {
+  const uint32_t t = threadIdx.x, T = blockDim.x, per = kB / T;  // buckets a thread scans
+  uint32_t lo = 0xffffffffu, hi = 0u;
+  for (uint32_t k = t; k < n; k += T) {
+    const uint32_t id = slot[s0 + k];
+    lo = min(lo, id);
+    hi = max(hi, id);
+  }
+  lo = block_min_max(lo, false, red);
+  hi = block_min_max(hi, true, red);
+  const float scale = (float)kB / ((float)(hi - lo) + 1.f);
+  auto bucket = [&](uint32_t id) { return min((uint32_t)((float)(id - lo) * scale), kB - 1u); };
+  for (uint32_t k = t; k < rank_padded(kB); k += T) hist[k] = 0u;
+  __syncthreads();
+  for (uint32_t k = t; k < n; k += T) atomicAdd(&hist[rank_slot(bucket(slot[s0 + k]))], 1u);
+  __syncthreads();
+  uint32_t sum = 0u, most = 0u;
+  for (uint32_t j = 0; j < per; ++j) {
+    const uint32_t c = hist[rank_slot(t * per + j)];
+    sum += c;
+    most = max(most, c);
+  }
+  if (block_min_max(most, true, red) > kRankBucketMax) return false;
+  uint32_t run = block_excl_scan(sum, red);
+  for (uint32_t j = 0; j < per; ++j) {
+    const uint32_t c = hist[rank_slot(t * per + j)];
+    hist[rank_slot(t * per + j)] = run;
+    run += c;
+  }
+  __syncthreads();
+  // into the buckets' ranges; afterwards hist[bucket b] = the end of b
+  for (uint32_t k = t; k < n; k += T) {
+    const uint32_t id = slot[s0 + k];
+    tmp[atomicAdd(&hist[rank_slot(bucket(id))], 1u)] = id;
+  }
+  __syncthreads();
+  for (uint32_t k = t; k < n; k += T) {
+    const uint32_t id = slot[s0 + k], b = bucket(id);
+    const uint32_t b0 = b ? hist[rank_slot(b - 1u)] : 0u, b1 = hist[rank_slot(b)];
+    uint32_t r = b0;
+    for (uint32_t u = b0; u < b1; ++u) r += tmp[u] < id;
+    dest_of[id] = s0 + r;
+  }
+  __syncthreads();  // hist and tmp are reused by the next segment
+  return true;
+}
+
+// Bitonic sort of one segment by the block, in `buf` (pow2_at_least(n)
+// words of shared memory) or, for larger segments, in `scratch` (2 words
+// per key at 2 * s0, so padded segments never overlap).
+__device__ __forceinline__ void block_sort_segment(uint32_t* __restrict__ slot, uint32_t s0, uint32_t n,
+                                                   uint32_t* buf, uint32_t buf_words, uint32_t* __restrict__ scratch,
+                                                   uint32_t* __restrict__ dest_of) {
+  const uint32_t m = pow2_at_least(n);
+  uint32_t* b = m <= buf_words ? buf : scratch + 2 * (size_t)s0;
+  for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) b[k] = k < n ? slot[s0 + k] : 0xffffffffu;
+  __syncthreads();
+  if (m <= buf_words)
+    bitonic(b, m, threadIdx.x, blockDim.x, [] { __syncthreads(); });
+  else
+    bitonic(b, m, threadIdx.x, blockDim.x, [] {
+      __threadfence_block();
+      __syncthreads();
+    });
+  for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+    if (dest_of) dest_of[b[k]] = s0 + k;
+    else slot[s0 + k] = b[k];
+  }
+  __syncthreads();
+}
+
+// The listed cells of up to kWarpSortMax ids: ranked by buckets, or sorted
+// by the block when their ids bunch.
+__global__ void __launch_bounds__(kRankThreads)
+k_rank_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
+             uint32_t* __restrict__ slot, const uint32_t* __restrict__ list,
+             const uint32_t* __restrict__ counters, uint32_t* __restrict__ dest_of) {
+  __shared__ uint32_t hist[rank_padded(kRankBuckets)], tmp[kWarpSortMax], red[32];
+  const uint32_t nl = counters[0];
+  for (uint32_t q = blockIdx.x; q < nl; q += gridDim.x) {
+    const uint32_t c = list[q], s0 = start[c], n = count[c];
+    if (!block_rank_segment<kRankBuckets>(slot, s0, n, dest_of, hist, tmp, red))
+      block_sort_segment(slot, s0, n, tmp, kWarpSortMax, nullptr, dest_of);
   }
 }
+
+// The listed cells above kWarpSortMax ids: ranked by buckets up to
+// kBlockSortMax ids, sorted otherwise (in shared memory up to kBlockSortMax,
+// through `scratch` beyond).  Dynamic shared memory: kBigRankSmem bytes.
+constexpr size_t kBigRankSmem = (kBlockSortMax + rank_padded(kBigRankBuckets) + 32) * sizeof(uint32_t);
+__global__ void __launch_bounds__(kBigThreads)
+k_rank_big_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,
+                 uint32_t* __restrict__ slot, const uint32_t* __restrict__ big_list,
+                 const uint32_t* __restrict__ big_count, uint32_t* __restrict__ scratch,
+                 uint32_t* __restrict__ dest_of) {
+  extern __shared__ uint32_t sbuf[];
+  uint32_t* tmp = sbuf;
+  uint32_t* hist = sbuf + kBlockSortMax;
+  uint32_t* red = hist + rank_padded(kBigRankBuckets);
+  const uint32_t nbig = *big_count;
+  for (uint32_t q = blockIdx.x; q < nbig; q += gridDim.x) {
+    const uint32_t c = big_list[q], n = count[c], s0 = start[c];
+    if (n <= kBlockSortMax && block_rank_segment<kBigRankBuckets>(slot, s0, n, dest_of, hist, tmp, red))
+      continue;
+    block_sort_segment(slot, s0, n, tmp, kBlockSortMax, scratch, dest_of);
+  }
+}
+static_assert(kRankBuckets % kRankThreads == 0 && kBigRankBuckets % kBigThreads == 0, "buckets per thread");
 
 __global__ void __launch_bounds__(kBigThreads)
 k_sort_big_cells(const uint32_t* __restrict__ start, const uint32_t* __restrict__ count,

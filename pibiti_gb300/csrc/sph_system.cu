@@ -19,8 +19,9 @@
 //   exclusive scan     count -> start, and the lists of the cells with
 //                      more than 32 particles
 //   k_scatter_ids      slot[start + rank] = original index
-//   k_sort_cells,      the id segments of the listed cells sorted (a warp,
-//   k_sort_big_cells   a block, or a block over global scratch, by size)
+//   k_rank_cells,      each listed cell's ids ranked by buckets (a block per
+//   k_rank_big_cells   cell; sorted instead where they bunch), the latter for
+//                      cells above 1024 ids, on a side stream
 //   k_place            stable position inside the cell = number of smaller
 //                      original indices there (the reference's sort is
 //                      stable on original order); integrate again and write
@@ -1378,13 +1379,13 @@ int enqueue_step(SphSystem* s, cudaStream_t st, cudaEvent_t* ev = nullptr,
   // the two kernels sort disjoint cells
   SPH_CUDA(cudaEventRecord(s->fork_ev, st), "step: fork");
   SPH_CUDA(cudaStreamWaitEvent(s->side, s->fork_ev, 0), "step: fork");
-  k_sort_big_cells<<<s->big_blocks, kBigThreads, kBlockSortMax * sizeof(uint32_t), s->side>>>(
+  k_rank_big_cells<<<s->big_blocks, kBigThreads, kBigRankSmem, s->side>>>(
       s->start, s->count, s->slot, s->big_list, s->sort_counters + 1, s->sort_scratch, s->dest);
   SPH_CUDA(cudaEventRecord(s->join_ev, s->side), "step: join");
   // cells of up to kWarpSortMax ids: ranked by buckets (k_rank_cells; the
-  // few whose ids bunch into one bucket are sorted by the same warp)
-  k_rank_cells<<<s->sort_blocks, kRankWarps * 32, 0, st>>>(s->start, s->count, s->slot, s->sort_list,
-                                                          s->sort_counters, s->dest);
+  // few whose ids bunch into one bucket are sorted by the same block)
+  k_rank_cells<<<s->sort_blocks, kRankThreads, 0, st>>>(s->start, s->count, s->slot, s->sort_list,
+                                                        s->sort_counters, s->dest);
   SPH_CUDA(cudaStreamWaitEvent(st, s->join_ev, 0), "step: join");
   mark();
   k_place<<<gN, kBlock, 0, st>>>(sc, s->d_poff, s->S, s->N, s->pos[a], s->vel[v], s->id[a],
@@ -1509,9 +1510,9 @@ int create(const SimParams* scenes, uint32_t count, SphSystem** out) {
   if (rc == SPH_OK) rc = cuda_check(cudaEventCreateWithFlags(&s->fork_ev, cudaEventDisableTiming), "fork event");
   if (rc == SPH_OK) rc = cuda_check(cudaEventCreateWithFlags(&s->join_ev, cudaEventDisableTiming), "join event");
   if (rc == SPH_OK)
-    rc = cuda_check(cudaFuncSetAttribute(k_sort_big_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(kBlockSortMax * sizeof(uint32_t))),
-                    "crowded-cell sort shared memory");
+    rc = cuda_check(cudaFuncSetAttribute(k_rank_big_cells, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kBigRankSmem),
+                    "crowded-cell ranking shared memory");
   if (rc == SPH_OK) rc = tile_attributes();
   if (rc == SPH_OK) {
     int dev = 0, sms = 1;
