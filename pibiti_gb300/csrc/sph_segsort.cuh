@@ -1,7 +1,9 @@
 // sph_segsort.cuh -- sorting many independent segments of uint32 keys
 // (segment k: data[start[k], start[k] + count[k])), used for the ids of
-// crowded grid cells and for the renderer's per-tile sprite lists.
-// Three kernels:
+// crowded grid cells and for the renderer's per-tile sprite lists, and
+// ranking segments of distinct ids (k_rank_cells, k_rank_big_cells, below:
+// the crowded cells of the step, which only need each id's rank).
+// The sorting kernels:
 //   k_find_cells      segments longer than `min_sort` go to `list` (up to
 //                     kWarpSortMax) or `big_list`, one atomic per warp and list
 //   k_sort_cells      one warp per listed segment: bitonic in registers
