@@ -514,18 +514,19 @@ def test_cell_sort_size_boundaries(cuda):
     np.testing.assert_array_equal(cs, o["cell_start"])
 
 
-def test_cell_ranks_with_bunched_ids(cuda):
-    """A cell whose ids bunch at one end of their range (ids 0..1000 and
-    99,999 together): the bucket ranking sorts it instead, and a cell of
-    spread ids next to it is ranked by buckets; both come out in
+@pytest.mark.parametrize("n,nb", [(100_000, 1001), (200_000, 2000)])
+def test_cell_ranks_with_bunched_ids(cuda, n, nb):
+    """A cell whose ids bunch at one end of their range (ids 0..nb-1 and
+    n-1 together; nb = 2000 makes it a cell above 1024 ids, ranked per
+    block with 4096 buckets): the bucket ranking sorts it instead, and a
+    cell of spread ids next to it is ranked by buckets; both come out in
     (hash, original index) order."""
     rng = np.random.default_rng(21)
     h = configs.H_DAMBREAK
-    n = 100_000
     pos = np.ones((n, 4), np.float32)
     pos[:, :3] = rng.uniform(0.05, 0.95, size=(n, 3))
     lo = np.array([6.35, 6.35, 6.35]) * h  # inside one cell, away from its faces
-    bunch = np.r_[np.arange(1001), n - 1]
+    bunch = np.r_[np.arange(nb), n - 1]
     pos[bunch, :3] = rng.uniform(lo, lo + 0.3 * h, (len(bunch), 3))
     spread = rng.choice(np.arange(2000, n - 1), 700, replace=False)
     lo2 = lo + np.array([2.0, 0.0, 0.0]) * h
@@ -539,7 +540,7 @@ def test_cell_ranks_with_bunched_ids(cuda):
     o = oracle.full_stages(p, pos, vel)
     cnt = np.bincount(o["sorted"][:, 0], minlength=p.numCells)
     top = sorted(cnt)[-2:]  # the two cells, with a few of the spread particles
-    assert 700 <= top[0] <= 1024 and 1002 <= top[1] <= 1024
+    assert 700 <= top[0] <= 1024 and nb + 1 <= top[1] <= nb + 100
     np.testing.assert_array_equal(sh, o["sorted"])
     np.testing.assert_array_equal(cs, o["cell_start"])
 
